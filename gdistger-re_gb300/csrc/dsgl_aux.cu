@@ -1,0 +1,174 @@
+// dsgl_aux.cu -- set-up kernels (Wih initialisation, corpus mapping), the explicit-row
+// minibatch update, and the SGNS loss with its hand-written adjoint.
+#include <cuda_runtime.h>
+
+#include "dsgl_device.cuh"
+
+namespace sgns {
+
+namespace {
+
+// InitNet (dsgl.hpp:451-456): element i of Wih takes LCG state r_{i+1} (r_0 = 1),
+// value ((r & 0xFFFF) / 65536 - 0.5) / d.  Each thread owns 64 consecutive elements and
+// starts from a jump-ahead; bf16 tables store the fp32 value rounded to nearest even.
+__global__ void init_wih_kernel(void* wih, int storage, int64_t n, int32_t d, const LcgJumps* J) {
+  const int64_t i0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 64;
+  if (i0 >= n) return;
+  uint64_t r = jump_any(1ULL, (uint64_t)i0, J);
+  const float fd = (float)d;
+  for (int k = 0; k < 64 && i0 + k < n; k++) {
+    r = lcg_next(r);
+    const float v = __fdiv_rn(__fsub_rn(__fdiv_rn((float)(uint32_t)(r & 0xFFFF), 65536.0f), 0.5f), fd);
+    if (storage == STORE_BF16)
+      static_cast<__nv_bfloat16*>(wih)[i0 + k] = __float2bfloat16_rn(v);
+    else
+      static_cast<float*>(wih)[i0 + k] = v;
+  }
+}
+
+// vertex ids -> sorted rows; -1 separators kept; anything else outside [0, V) flagged
+__global__ void map_corpus_kernel(const int32_t* ids, const int32_t* row_of, int32_t* rows, int64_t n,
+                                  int64_t V, int32_t* bad) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t t = ids[i];
+    if (t == -1) {
+      rows[i] = -1;
+    } else if (t < 0 || (int64_t)t >= V) {
+      rows[i] = -1;
+      atomicExch(bad, 1);
+    } else {
+      rows[i] = row_of[t];
+    }
+  }
+}
+
+// ---- explicit-row minibatch update (the step arithmetic of both trainers) ----------
+template <int DCH>
+__global__ void __launch_bounds__(32) minibatch_kernel(int d, int imax, int omax, const int32_t* in_count,
+                                                       const int32_t* in_first, const int32_t* out_count,
+                                                       const int32_t* out_meta_all, const float* alpha,
+                                                       const int64_t* in_off, const int64_t* out_off,
+                                                       const float* in_rows, const float* out_rows,
+                                                       float* d_in, float* d_out, const float* exp_table,
+                                                       int32_t* status) {
+  extern __shared__ __align__(16) float smem[];
+  const int b = blockIdx.x, lane = lane_id();
+  const int I = in_count[b], first = in_first[b], O = out_count[b];
+  if (I < 1 || I > imax || O < 2 || O > omax || first < 0 || first > I) {
+    if (lane == 0) atomicExch(status, 1);
+    return;
+  }
+  const int DP = d + 4, OP = (omax + 3) & ~3;
+  float* exp_s = smem;
+  float* xin = smem + 1004;
+  float* xout = xin + (size_t)imax * DP;
+  float* corrT = xout + (size_t)omax * DP;
+  int* meta = reinterpret_cast<int*>(corrT + (size_t)imax * OP);
+  for (int i = lane; i < kExpTableSize + 1; i += 32) exp_s[i] = exp_table[i];
+  const int d4 = d >> 2;
+  const float* gin = in_rows + in_off[b] * d;
+  const float* gout = out_rows + out_off[b] * d;
+  for (int j = 0; j < I; j++)
+    for (int q = lane; q < d4; q += 32)
+      reinterpret_cast<float4*>(xin + (size_t)j * DP)[q] = reinterpret_cast<const float4*>(gin + (size_t)j * d)[q];
+  for (int i = 0; i < O; i++)
+    for (int q = lane; q < d4; q += 32)
+      reinterpret_cast<float4*>(xout + (size_t)i * DP)[q] = reinterpret_cast<const float4*>(gout + (size_t)i * d)[q];
+  for (int i = lane; i < O; i += 32) meta[i] = out_meta_all[out_off[b] + i];
+  __syncwarp();
+  auto in_ptr = [&](int j) -> const float* { return xin + (size_t)j * DP; };
+  float loss = 0.f;
+  forward_gradient(I, first, O, d, in_ptr, xout, DP, meta, exp_s, alpha[b], corrT, OP, false, loss);
+  float4 md[kOMax][DCH];
+  float* gdin = d_in + in_off[b] * d;
+  backward<DCH>(I, O, d, in_ptr, xout, DP, corrT, OP, md,
+                [&](int j, int q, float4 a) { reinterpret_cast<float4*>(gdin + (size_t)j * d)[q] = a; });
+  float* gdout = d_out + out_off[b] * d;
+#pragma unroll
+  for (int i = 0; i < kOMax; i++)
+#pragma unroll
+    for (int t = 0; t < DCH; t++) {
+      const int q = lane + 32 * t;
+      if (i < O && q < d4) reinterpret_cast<float4*>(gdout + (size_t)i * d)[q] = md[i][t];
+    }
+}
+
+// each walk start scans forward to its separator (at most kMaxSentence tokens)
+__global__ void max_walk_kernel(const int32_t* rows, int64_t n, int32_t* out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    if (rows[i] == -1 || (i > 0 && rows[i - 1] != -1)) continue;
+    int len = 0;
+    while (i + len < n && rows[i + len] != -1 && len < kMaxSentence) len++;
+    atomicMax(out, len);
+  }
+}
+
+__global__ void prefix_offsets_kernel(const int32_t* cnt_a, const int32_t* cnt_b, int n, int64_t* off_a,
+                                      int64_t* off_b) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    int64_t a = 0, bb = 0;
+    for (int i = 0; i < n; i++) {
+      off_a[i] = a;
+      off_b[i] = bb;
+      a += cnt_a[i];
+      bb += cnt_b[i];
+    }
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_init_wih(void* wih, int storage, int64_t V, int32_t d, const LcgJumps* jumps,
+                            cudaStream_t s) {
+  const int64_t n = V * d;
+  const int64_t threads = (n + 63) / 64;
+  init_wih_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(wih, storage, n, d, jumps);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_map_corpus(const int32_t* ids, const int32_t* row_of, int32_t* rows, int64_t n,
+                              int64_t V, int32_t* bad, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  map_corpus_kernel<<<(unsigned)blocks, 256, 0, s>>>(ids, row_of, rows, n, V, bad);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_max_walk(const int32_t* rows, int64_t n, int32_t* out, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  max_walk_kernel<<<(unsigned)blocks, 256, 0, s>>>(rows, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_minibatch(int d, int n, int imax, int omax, const int32_t* in_count,
+                             const int32_t* in_first, const int32_t* out_count, const int32_t* out_meta,
+                             const float* alpha, const float* in_rows, const float* out_rows, float* d_in,
+                             float* d_out, const float* exp_table, int64_t* offsets, int32_t* status,
+                             cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  int64_t* in_off = offsets;
+  int64_t* out_off = offsets + n;
+  prefix_offsets_kernel<<<1, 1, 0, s>>>(in_count, out_count, n, in_off, out_off);
+  const int DP = d + 4, OP = (omax + 3) & ~3;
+  const size_t smem = sizeof(float) * (1004 + (size_t)(imax + omax) * DP + (size_t)imax * OP + omax + 4);
+  cudaError_t e;
+  if (d > 128) {
+    e = cudaFuncSetAttribute(minibatch_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    minibatch_kernel<2><<<n, 32, smem, s>>>(d, imax, omax, in_count, in_first, out_count, out_meta, alpha,
+                                            in_off, out_off, in_rows, out_rows, d_in, d_out, exp_table, status);
+  } else {
+    e = cudaFuncSetAttribute(minibatch_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    minibatch_kernel<1><<<n, 32, smem, s>>>(d, imax, omax, in_count, in_first, out_count, out_meta, alpha,
+                                            in_off, out_off, in_rows, out_rows, d_in, d_out, exp_table, status);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace sgns

@@ -1,0 +1,368 @@
+// dsgl_window.cu -- the persistent DSGL engine (SGNS_ENGINE_PERSISTENT).
+//
+// One warp is one worker: the GPU counterpart of one compute thread of the reference's
+// Train_SGNS_MPI (include/dsgl.hpp:783-1425).  A single launch runs every worker over
+// its contiguous corpus slice (dsgl.hpp:811-826) for -iter passes, whatever the walk
+// lengths, with no host round trip.  Per worker, shared memory holds
+//   * the two walks in flight (rows after subsampling),
+//   * their context rows while any position of the row lies in the sliding window
+//     [pos-w, pos+w] -- one fp32 copy per distinct vertex per walk, exactly the
+//     reference's per-walk deduplicated buffer, loaded when it enters the window and
+//     written back (stochastically rounded for bf16 tables) when it leaves it,
+//   * the step's output rows (target of each walk + shared negatives) and gradients.
+// Negative rows are read from and added to Woh at each step, as the reference does for
+// the two target rows (dsgl.hpp:1346-1356).  The negative pool keeps the reference's
+// draw stream (max(len1,len2)*K draws per pool, group neg_count % n per step,
+// dsgl.hpp:1054-1073, 1136-1154) but is regenerated from its base LCG state instead of
+// being stored.
+#include <cuda_runtime.h>
+
+#include "dsgl_device.cuh"
+
+namespace sgns {
+
+namespace {
+
+constexpr int kHdrWords = 1004 + 132;  // sigmoid table (1001 -> 1004) + SmallJumps (528 B)
+
+struct WinLayout {  // per-warp shared memory, in 4-byte words
+  int NS, R, DP, OP, OM, IM, lmax;
+  int rows, corr, sen, vert, ref, ring, inrow, outid, outmeta, words;
+};
+
+__host__ __device__ inline WinLayout win_layout(int d, int w, int K, int lmax) {
+  WinLayout L;
+  L.NS = 2 * w + 2;  // resident slots per walk (2w+1 positions, +1 while a row enters)
+  L.R = 2 * w + 2;   // ring of position -> slot
+  L.DP = d + 4;      // padded row stride: 32 lanes reading 32 rows hit 32 distinct banks
+  L.OM = K + 2;
+  L.OP = (L.OM + 3) & ~3;
+  L.IM = 4 * w;
+  L.lmax = lmax;
+  int off = 0;
+  L.rows = off;
+  off += (2 * L.NS + L.OM) * L.DP;
+  L.corr = off;
+  off += L.IM * L.OP;
+  L.sen = off;
+  off += 2 * lmax;
+  L.vert = off;
+  off += 2 * L.NS;
+  L.ref = off;
+  off += 2 * L.NS;
+  L.ring = off;
+  off += 2 * L.R;
+  L.inrow = off;
+  off += L.IM;
+  L.outid = off;
+  off += L.OM;
+  L.outmeta = off;
+  off += L.OM;
+  L.words = (off + 3) & ~3;
+  return L;
+}
+
+template <int S>
+__device__ __forceinline__ void load_row_to_smem(const void* tab, int64_t row, int d, float* dst) {
+  const int d4 = d >> 2;
+  for (int q = lane_id(); q < d4; q += 32)
+    reinterpret_cast<float4*>(dst)[q] = RowIO<S>::load4(tab, row, d, q);
+}
+template <int S>
+__device__ __forceinline__ void store_row_from_smem(void* tab, int64_t row, int d, const float* src,
+                                                    uint64_t ev) {
+  const int d4 = d >> 2;
+  for (int q = lane_id(); q < d4; q += 32)
+    RowIO<S>::store4(tab, row, d, q, reinterpret_cast<const float4*>(src)[q], ev);
+}
+
+template <int S, int DCH>
+__global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
+  extern __shared__ __align__(16) float smem[];
+  float* exp_s = smem;
+  SmallJumps* sj = reinterpret_cast<SmallJumps*>(smem + 1004);
+  for (int i = threadIdx.x; i < kExpTableSize + 1; i += blockDim.x) exp_s[i] = p.exp_table[i];
+  for (int i = threadIdx.x; i < 33; i += blockDim.x) {
+    sj->mul[i] = p.jumps->small_mul[i];
+    sj->add[i] = p.jumps->small_add[i];
+  }
+  __syncthreads();
+
+  const int lane = lane_id();
+  const int wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (wid >= p.workers) return;
+
+  const int d = p.d, w = p.window, K = p.K;
+  const WinLayout L = win_layout(d, w, K, p.lmax);
+  float* base = smem + kHdrWords + (threadIdx.x >> 5) * L.words;
+  float* rows = base + L.rows;
+  float* out_rows = rows + (size_t)2 * L.NS * L.DP;
+  float* corrT = base + L.corr;
+  int* sen = reinterpret_cast<int*>(base + L.sen);
+  int* vert = reinterpret_cast<int*>(base + L.vert);
+  int* ref = reinterpret_cast<int*>(base + L.ref);
+  int* ring = reinterpret_cast<int*>(base + L.ring);
+  int* in_row = reinterpret_cast<int*>(base + L.inrow);
+  int* out_id = reinterpret_cast<int*>(base + L.outid);
+  int* out_meta = reinterpret_cast<int*>(base + L.outmeta);
+  const int NS = L.NS, R = L.R, DP = L.DP, lmax = L.lmax;
+
+  // dsgl.hpp:790-826
+  uint64_t rng = (uint64_t)wid, word_count = 0, last_wc = 0, step_id = 0;
+  const uint64_t words_num = (uint64_t)p.words_num, parts = (uint64_t)p.workers;
+  uint64_t tw = words_num / parts;
+  const int64_t start = (int64_t)(tw * (uint64_t)wid);
+  if (words_num % parts > 0 && (uint64_t)wid == parts - 1) tw = words_num - (parts - 1) * tw;
+  const int64_t end = start + (int64_t)tw;
+  int64_t cur = start;
+  int local_iter = p.iter;
+  int len[2] = {0, 0}, pos[2] = {0, 0};
+  int train_sen_num = 0, neg_count = 0, neg_n = 1, grp_g = -1;
+  bool change_neg = true;
+  uint64_t pool_base = 0, grp_state = 0;
+  for (int s = lane; s < 2 * NS; s += 32) ref[s] = 0;
+  float loss = 0.f;
+  unsigned long long n_pairs = 0, n_steps = 0, n_outs = 0, n_loads = 0, n_stores = 0;
+  __syncwarp();
+
+  auto enter = [&](int walk, int position) -> bool {  // true if a row must be loaded
+    const int v = sen[walk * lmax + position];
+    int* wref = ref + walk * NS;
+    int* wvert = vert + walk * NS;
+    const unsigned hit = __ballot_sync(kFull, lane < NS && wref[lane] > 0 && wvert[lane] == v);
+    int s;
+    bool fresh = false;
+    if (hit) {
+      s = __ffs(hit) - 1;
+    } else {
+      const unsigned fr = __ballot_sync(kFull, lane < NS && wref[lane] == 0);
+      s = __ffs(fr) - 1;
+      fresh = true;
+    }
+    __syncwarp();
+    if (lane == 0) {
+      if (fresh) wvert[s] = v;
+      wref[s] += 1;
+      ring[walk * R + position % R] = s;
+    }
+    __syncwarp();
+    if (fresh) {
+      load_row_to_smem<S>(p.wih, v, d, rows + (size_t)(walk * NS + s) * DP);
+      n_loads++;
+    }
+    return fresh;
+  };
+  auto leave = [&](int walk, int position, uint64_t ev) {
+    const int s = ring[walk * R + position % R];
+    const int r = ref[walk * NS + s] - 1;
+    const int v = vert[walk * NS + s];
+    __syncwarp();
+    if (lane == 0) ref[walk * NS + s] = r;
+    if (r == 0) {
+      store_row_from_smem<S>(p.wih, v, d, rows + (size_t)(walk * NS + s) * DP, ev);
+      n_stores++;
+    }
+    __syncwarp();
+  };
+  auto flush_walk = [&](int walk, uint64_t ev) {
+    for (int s = 0; s < NS; s++) {
+      const int r = ref[walk * NS + s];
+      if (r > 0) {
+        store_row_from_smem<S>(p.wih, vert[walk * NS + s], d, rows + (size_t)(walk * NS + s) * DP, ev);
+        n_stores++;
+      }
+    }
+    __syncwarp();
+    for (int s = lane; s < NS; s += 32) ref[walk * NS + s] = 0;
+    __syncwarp();
+  };
+
+  while (true) {
+    if (word_count - last_wc > 10000) {  // dsgl.hpp:886-897
+      const uint64_t diff = word_count - last_wc;
+      if (lane == 0) {
+        unsigned long long now = atomicAdd(&p.ctr->wca, (unsigned long long)diff) + diff;
+        *reinterpret_cast<volatile float*>(&p.ctr->alpha) = alpha_update(p, now);
+      }
+      last_wc = word_count;
+      __syncwarp();
+    }
+    for (int walk = 0; walk < 2; walk++) {  // dsgl.hpp:902-1030
+      while (len[walk] == 0) {
+        if (cur >= end) break;
+        const int n = fill_walk(p, *sj, sen + walk * lmax, cur, end, word_count, rng, lmax);
+        if (n <= 1) continue;
+        len[walk] = n;
+        pos[walk] = 0;
+        const int hi = n - 1 < w ? n - 1 : w;
+        for (int q = 0; q <= hi; q++) enter(walk, q);
+      }
+    }
+    if (cur >= end) {  // dsgl.hpp:1031-1050
+      if (lane == 0) atomicAdd(&p.ctr->wca, (unsigned long long)(word_count - last_wc));
+      if (--local_iter == 0) break;
+      word_count = 0;
+      last_wc = 0;
+      cur = start;
+      len[0] = len[1] = 0;
+      for (int s = lane; s < 2 * NS; s += 32) ref[s] = 0;
+      __syncwarp();
+      continue;
+    }
+    if (change_neg) {  // dsgl.hpp:1054-1088: the pool is its base state and size
+      pool_base = rng;
+      neg_n = len[0] > len[1] ? len[0] : len[1];
+      rng = jump_any(rng, (uint64_t)neg_n * (uint64_t)K, p.jumps);
+      change_neg = false;
+      grp_g = -1;
+    }
+
+    // ---- one step (dsgl.hpp:1089-1368) ----
+    const int t1 = sen[pos[0]], t2 = sen[lmax + pos[1]];
+    rng = lcg_next(rng);
+    const int b = (int)fast_mod(rng, p.div_window);
+    const int I0 = window_inputs(pos[0], len[0], w, b, 0, in_row,
+                                 [&](int c) { return ring[c % R]; });
+    const int I = I0 + window_inputs(pos[1], len[1], w, b, I0, in_row,
+                                     [&](int c) { return NS + ring[R + c % R]; });
+    neg_count++;
+    const int g = neg_count % neg_n;
+    uint64_t gs;
+    if (g == 0) gs = pool_base;
+    else if (g == grp_g + 1) gs = jump_small(grp_state, K, *sj);
+    else gs = jump_any(pool_base, (uint64_t)g * (uint64_t)K, p.jumps);
+    grp_g = g;
+    grp_state = gs;
+    const int O = select_outputs(p, *sj, gs, t1, t2, out_id, out_meta);
+    {  // gather the output rows (targets and negatives) from Woh
+      const int d4 = d >> 2;
+      for (int i = 0; i < O; i++) {
+        const int row = out_id[i];
+        for (int q = lane; q < d4; q += 32)
+          reinterpret_cast<float4*>(out_rows + (size_t)i * DP)[q] = RowIO<S>::load4(p.woh, row, d, q);
+      }
+    }
+    __syncwarp();
+    const float alpha = *reinterpret_cast<volatile float*>(&p.ctr->alpha);
+    auto in_ptr = [&](int j) -> const float* { return rows + (size_t)in_row[j] * DP; };
+    forward_gradient(I, I0, O, d, in_ptr, out_rows, DP, out_meta, exp_s, alpha, corrT, L.OP,
+                     p.compute_loss != 0, loss);
+    float4 md[kOMax][DCH];
+    backward<DCH>(I, O, d, in_ptr, out_rows, DP, corrT, L.OP, md, add_to_input(in_ptr));
+    {  // Woh += outputMd: target 1, target 2, then each negative (aliases follow that order)
+      uint64_t e1 = 0, e2 = 0, en = 0;
+      if (S == STORE_BF16) {
+        e1 = sr_event_key(p.sr_seed, EV_TARGET1, (uint32_t)wid, step_id);
+        e2 = sr_event_key(p.sr_seed, EV_TARGET2, (uint32_t)wid, step_id);
+        en = sr_event_key(p.sr_seed, EV_NEG, (uint32_t)wid, step_id);
+      }
+      const int d4 = d >> 2;
+#pragma unroll
+      for (int t = 0; t < DCH; t++) {
+        const int q = lane + 32 * t;
+        if (q < d4) {
+          float4 mlast = md[0][t];
+#pragma unroll
+          for (int i = 1; i < kOMax; i++)
+            if (i == O - 1) mlast = md[i][t];
+          const float4 b1 = reinterpret_cast<const float4*>(out_rows)[q];
+          const float4 n1 = RowIO<S>::store4(p.woh, t1, d, q, add4(b1, md[0][t]), e1);
+          const float4 b2 = t2 == t1 ? n1
+                                     : reinterpret_cast<const float4*>(out_rows + (size_t)(O - 1) * DP)[q];
+          const float4 n2 = RowIO<S>::store4(p.woh, t2, d, q, add4(b2, mlast), e2);
+#pragma unroll
+          for (int i = 1; i < kOMax - 1; i++) {
+            if (i < O - 1) {
+              const int row = out_id[i];
+              const float4 bi = row == t2 ? n2
+                                          : reinterpret_cast<const float4*>(out_rows + (size_t)i * DP)[q];
+              RowIO<S>::store4(p.woh, row, d, q, add4(bi, md[i][t]), en);
+            }
+          }
+        }
+      }
+    }
+    n_pairs += (unsigned long long)I;
+    n_outs += (unsigned long long)O;
+    n_steps++;
+    __syncwarp();
+
+    // ---- positions, window moves, walk ends (dsgl.hpp:1372-1407) ----
+    pos[0]++;
+    pos[1]++;
+    for (int walk = 0; walk < 2; walk++) {
+      const uint64_t ev =
+          S == STORE_BF16 ? sr_event_key(p.sr_seed, EV_WALK0 + walk, (uint32_t)wid, step_id) : 0;
+      if (pos[walk] >= len[walk]) {
+        flush_walk(walk, ev);
+        len[walk] = 0;
+        train_sen_num++;
+      } else {
+        const int P = pos[walk];
+        if (P + w < len[walk]) enter(walk, P + w);
+        if (P - w - 1 >= 0) leave(walk, P - w - 1, ev);
+      }
+    }
+    if (train_sen_num >= 2) {
+      change_neg = true;
+      train_sen_num = 0;
+    }
+    step_id++;
+  }
+
+  // worker statistics
+  if (p.compute_loss) {
+    for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(kFull, loss, o);
+  }
+  if (lane == 0) {
+    atomicAdd(&p.ctr->pairs, n_pairs);
+    atomicAdd(&p.ctr->steps, n_steps);
+    atomicAdd(&p.ctr->outputs, n_outs);
+    atomicAdd(&p.ctr->row_loads, n_loads);
+    atomicAdd(&p.ctr->row_stores, n_stores);
+    if (p.compute_loss) atomicAdd(&p.ctr->loss, (double)loss);
+    atomicSub(&p.ctr->active, 1);
+  }
+}
+
+}  // namespace
+
+size_t window_smem_bytes(int d, int window, int K, int lmax, int warps_per_cta) {
+  const WinLayout L = win_layout(d, window, K, lmax);
+  return sizeof(float) * ((size_t)kHdrWords + (size_t)warps_per_cta * L.words);
+}
+
+template <int S, int DCH>
+static cudaError_t occupancy_t(int d, int w, int K, int lmax, int wpc, int* ctas) {
+  const size_t smem = window_smem_bytes(d, w, K, lmax, wpc);
+  cudaError_t e = cudaFuncSetAttribute(window_engine_kernel<S, DCH>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas, window_engine_kernel<S, DCH>, 32 * wpc, smem);
+}
+
+cudaError_t window_engine_occupancy(int storage, int d, int w, int K, int lmax, int wpc, int* ctas) {
+  const bool wide = d > 128;
+  if (storage == STORE_BF16)
+    return wide ? occupancy_t<STORE_BF16, 2>(d, w, K, lmax, wpc, ctas) : occupancy_t<STORE_BF16, 1>(d, w, K, lmax, wpc, ctas);
+  return wide ? occupancy_t<STORE_F32, 2>(d, w, K, lmax, wpc, ctas) : occupancy_t<STORE_F32, 1>(d, w, K, lmax, wpc, ctas);
+}
+
+template <int S, int DCH>
+static cudaError_t launch_t(const TrainParams& p, int wpc, cudaStream_t s) {
+  const size_t smem = window_smem_bytes(p.d, p.window, p.K, p.lmax, wpc);
+  cudaError_t e = cudaFuncSetAttribute(window_engine_kernel<S, DCH>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const int blocks = (p.workers + wpc - 1) / wpc;
+  window_engine_kernel<S, DCH><<<blocks, 32 * wpc, smem, s>>>(p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_window_engine(const TrainParams& p, int wpc, cudaStream_t s) {
+  const bool wide = p.d > 128;
+  if (p.storage == STORE_BF16) return wide ? launch_t<STORE_BF16, 2>(p, wpc, s) : launch_t<STORE_BF16, 1>(p, wpc, s);
+  return wide ? launch_t<STORE_F32, 2>(p, wpc, s) : launch_t<STORE_F32, 1>(p, wpc, s);
+}
+
+}  // namespace sgns

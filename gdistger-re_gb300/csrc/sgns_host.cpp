@@ -1,0 +1,929 @@
+// sgns_host.cpp -- the C ABI of include/sgns.h: options, vocabulary and tables, corpus
+// staging, engine dispatch, CUDA-graph capture of the persistent launch, the autotuner,
+// and the reference's text embedding output.
+//
+// Host-side set-up follows the reference's preparatory_work (include/dsgl.hpp:511-519):
+// vocabulary sort, unigram table, sigmoid table and subsampling thresholds are built
+// here once per vocabulary (the reference also builds them on the host); all training
+// work runs in the CUDA kernels.  There is no CPU training path.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/sgns.h"
+#include "sgns_internal.h"
+
+using namespace sgns;
+
+struct sgns_handle {
+  sgns_options opt{};
+  std::string err;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // vocabulary (host)
+  int64_t V = 0;
+  uint64_t train_words = 0;
+  std::vector<uint32_t> order;
+  std::vector<int32_t> row_of, cn_sorted;
+  // device state
+  void* wih = nullptr;
+  void* woh = nullptr;
+  int32_t* d_row_of = nullptr;
+  float* d_ran = nullptr;
+  int32_t* d_table = nullptr;
+  float* d_exp = nullptr;
+  LcgJumps* d_jumps = nullptr;
+  DeviceCounters* d_ctr = nullptr;
+  DeviceCounters* h_ctr = nullptr;  // pinned
+  int32_t* d_flags = nullptr;       // [0] bad id, [1] longest walk
+  int32_t* h_flags = nullptr;       // pinned
+  int32_t* d_ids = nullptr;
+  int32_t* d_corpus = nullptr;
+  int64_t n_tokens = 0, corpus_cap = 0;
+  int lmax = 0;
+  void* plain_scratch = nullptr;
+  size_t plain_bytes = 0;
+  // persistent engine launch shape and its captured graph
+  int workers = 0, wpc = 0;
+  bool tuned = false;
+  cudaGraphExec_t graph = nullptr;
+  std::string graph_key;
+  sgns_stats stats{};
+};
+
+namespace {
+
+std::mutex g_create_err_mx;
+std::string g_create_err;
+
+sgns_status fail(sgns_handle* h, sgns_status st, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (h) h->err = buf;
+  else {
+    std::lock_guard<std::mutex> g(g_create_err_mx);
+    g_create_err = buf;
+  }
+  return st;
+}
+
+#define CU(h, call)                                                                          \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess)                                                                   \
+      return fail((h), SGNS_ECUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_),   \
+                  __FILE__, __LINE__);                                                       \
+  } while (0)
+
+template <class T>
+void dfree(T*& p) {
+  if (p) cudaFree((void*)p);
+  p = nullptr;
+}
+
+size_t elem_bytes(const sgns_options& o) { return o.storage == SGNS_STORE_BF16_SR ? 2 : 4; }
+
+// ---- the reference's host set-up, restated (dsgl.hpp:121-147, 246-252, 314-382) ----
+struct VocabVertex {
+  int cn;
+  uint32_t id;
+};
+
+void build_unigram_table(const std::vector<int32_t>& cn, int64_t table_size, int threads,
+                         std::vector<int32_t>& table) {
+  const int64_t V = (int64_t)cn.size();
+  const float power = 0.75f;
+  if (threads < 1) threads = 1;
+  // OpenMP static-schedule reduction of dsgl.hpp:127-132: per-thread contiguous
+  // partial sums, combined in thread order.
+  double twp = 0.;
+  const int64_t q = V / threads, rem = V % threads;
+  for (int t = 0; t < threads; t++) {
+    const int64_t lo = t * q + std::min<int64_t>(t, rem);
+    const int64_t hi = lo + q + (t < rem ? 1 : 0);
+    double part = 0.;
+    for (int64_t i = lo; i < hi; i++) part += std::pow((double)cn[i], (double)power);
+    twp += part;
+  }
+  table.resize(table_size);
+  int64_t i = 0;
+  float d1 = (float)(std::pow((double)cn[0], (double)power) / twp);
+  for (int64_t a = 0; a < table_size; a++) {
+    table[a] = (int32_t)i;
+    if ((float)(int)a / (float)table_size > d1) {
+      i++;
+      if (i >= V) i = V - 1;
+      d1 = (float)((double)d1 + std::pow((double)cn[i], (double)power) / twp);
+    }
+  }
+}
+
+void build_exp_table(float* t) {  // dsgl.hpp:1557-1562
+  for (int i = 0; i < kExpTableSize + 1; i++) {
+    const float e = expf(((float)i / (float)kExpTableSize * 2 - 1) * kMaxExp);
+    t[i] = e / (e + 1);
+  }
+}
+
+sgns_status validate(sgns_handle* h, const sgns_options& o) {
+  if (o.size < 4 || o.size > kDMax || o.size % 4)
+    return fail(h, SGNS_EINVAL, "-size %d: must be a multiple of 4 in [4, %d]", o.size, kDMax);
+  if (o.window < 1 || o.window > kWMax - 1)
+    return fail(h, SGNS_EINVAL, "-window %d: must be in [1, %d]", o.window, kWMax - 1);
+  if (o.negative < 0 || o.negative > kKMax)
+    return fail(h, SGNS_EINVAL, "-negative %d: must be in [0, %d]", o.negative, kKMax);
+  if (o.iter < 1) return fail(h, SGNS_EINVAL, "-iter %d: must be >= 1", o.iter);
+  if (!(o.alpha >= 0.f) || !std::isfinite(o.alpha)) return fail(h, SGNS_EINVAL, "-alpha must be finite and >= 0");
+  if (!std::isfinite(o.sample)) return fail(h, SGNS_EINVAL, "-sample must be finite");
+  if (o.table_size < 1 || o.table_size > (int64_t)INT32_MAX)
+    return fail(h, SGNS_EINVAL, "table size %lld out of range", (long long)o.table_size);
+  if (o.storage != SGNS_STORE_FP32 && o.storage != SGNS_STORE_BF16_SR)
+    return fail(h, SGNS_EINVAL, "unknown storage %d", o.storage);
+  if (o.engine != SGNS_ENGINE_PLAIN && o.engine != SGNS_ENGINE_PERSISTENT)
+    return fail(h, SGNS_EINVAL, "unknown engine %d", o.engine);
+  if (o.workers < 0 || o.warps_per_cta < 0 || o.warps_per_cta > 8)
+    return fail(h, SGNS_EINVAL, "workers/warps_per_cta out of range");
+  return SGNS_OK;
+}
+
+TrainParams make_params(sgns_handle* h, int workers) {
+  TrainParams p{};
+  const sgns_options& o = h->opt;
+  p.corpus = h->d_corpus;
+  p.words_num = h->n_tokens;
+  p.ran = h->d_ran;
+  p.table = h->d_table;
+  p.exp_table = h->d_exp;
+  p.jumps = h->d_jumps;
+  p.wih = h->wih;
+  p.woh = h->woh;
+  p.div_table = make_fastdiv((uint64_t)o.table_size);
+  p.div_vm1 = make_fastdiv((uint64_t)(h->V - 1));
+  p.div_window = make_fastdiv((uint64_t)o.window);
+  p.V = h->V;
+  p.d = o.size;
+  p.window = o.window;
+  p.K = o.negative;
+  p.iter = o.iter;
+  p.workers = workers;
+  p.sample_on = o.sample > 0 ? 1 : 0;
+  p.start_alpha = o.alpha;
+  p.alpha_denom = (float)((uint64_t)o.iter * h->train_words + 1);  // dsgl.hpp:894
+  p.sr_seed = o.seed;
+  p.compute_loss = o.compute_loss;
+  p.lmax = h->lmax;
+  p.storage = o.storage == SGNS_STORE_BF16_SR ? STORE_BF16 : STORE_F32;
+  p.ctr = h->d_ctr;
+  return p;
+}
+
+sgns_status reset_counters(sgns_handle* h, int workers) {
+  DeviceCounters c{};
+  c.alpha = h->opt.alpha;
+  c.active = workers;
+  *h->h_ctr = c;
+  CU(h, cudaMemcpyAsync(h->d_ctr, h->h_ctr, sizeof c, cudaMemcpyHostToDevice, h->stream));
+  return SGNS_OK;
+}
+
+sgns_status finish_stats(sgns_handle* h, int workers, float ms) {
+  CU(h, cudaMemcpyAsync(h->h_ctr, h->d_ctr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost, h->stream));
+  CU(h, cudaStreamSynchronize(h->stream));
+  const DeviceCounters& c = *h->h_ctr;
+  if (c.status != 0) return fail(h, SGNS_EINVAL, "kernel reported a walk longer than the staged capacity");
+  sgns_stats& s = h->stats;
+  s.steps = c.steps;
+  s.pairs = c.pairs;
+  s.word_count_actual = c.wca;
+  s.row_bytes = 2ULL * (c.pairs + c.outputs) * (uint64_t)h->opt.size * elem_bytes(h->opt);
+  s.loss = c.loss;
+  s.final_alpha = c.alpha;
+  s.train_ms = ms;
+  s.workers = workers;
+  s.warps_per_cta = h->opt.engine == SGNS_ENGINE_PERSISTENT ? h->wpc : 4;
+  return SGNS_OK;
+}
+
+// largest worker count the persistent engine keeps resident in one wave
+sgns_status persistent_shape(sgns_handle* h, int wpc, int* workers) {
+  int ctas = 0;
+  const sgns_options& o = h->opt;
+  CU(h, window_engine_occupancy(o.storage == SGNS_STORE_BF16_SR ? STORE_BF16 : STORE_F32, o.size,
+                                o.window, o.negative, h->lmax, wpc, &ctas));
+  if (ctas < 1)
+    return fail(h, SGNS_EINVAL, "a %d-warp CTA does not fit in shared memory (d=%d, walks up to %d)", wpc,
+                o.size, h->lmax);
+  *workers = ctas * wpc * h->num_sms;
+  return SGNS_OK;
+}
+
+sgns_status run_persistent(sgns_handle* h, int workers, int wpc, bool use_graph, float* ms_out) {
+  TrainParams p = make_params(h, workers);
+  if (use_graph) {
+    char key[256];
+    snprintf(key, sizeof key, "%p/%lld/%d/%d/%p/%p/%d/%d", (void*)h->d_corpus, (long long)h->n_tokens,
+             workers, wpc, h->wih, h->woh, h->lmax, h->opt.iter);
+    if (!h->graph || h->graph_key != key) {
+      if (h->graph) cudaGraphExecDestroy(h->graph);
+      h->graph = nullptr;
+      DeviceCounters c{};
+      c.alpha = h->opt.alpha;
+      c.active = workers;
+      *h->h_ctr = c;
+      cudaGraph_t g;
+      CU(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+      cudaError_t e1 = cudaMemcpyAsync(h->d_ctr, h->h_ctr, sizeof c, cudaMemcpyHostToDevice, h->stream);
+      cudaError_t e2 = launch_window_engine(p, wpc, h->stream);
+      cudaError_t e3 = cudaStreamEndCapture(h->stream, &g);
+      if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess)
+        return fail(h, SGNS_ECUDA, "graph capture of the persistent launch failed: %s",
+                    cudaGetErrorString(e1 != cudaSuccess ? e1 : e2 != cudaSuccess ? e2 : e3));
+      cudaError_t e4 = cudaGraphInstantiate(&h->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (e4 != cudaSuccess) return fail(h, SGNS_ECUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e4));
+      h->graph_key = key;
+    }
+    // the captured host->device copy reads h_ctr at replay time: refresh it
+    DeviceCounters c{};
+    c.alpha = h->opt.alpha;
+    c.active = workers;
+    *h->h_ctr = c;
+    CU(h, cudaEventRecord(h->ev0, h->stream));
+    CU(h, cudaGraphLaunch(h->graph, h->stream));
+    CU(h, cudaEventRecord(h->ev1, h->stream));
+  } else {
+    sgns_status st = reset_counters(h, workers);
+    if (st) return st;
+    CU(h, cudaEventRecord(h->ev0, h->stream));
+    CU(h, launch_window_engine(p, wpc, h->stream));
+    CU(h, cudaEventRecord(h->ev1, h->stream));
+  }
+  CU(h, cudaEventSynchronize(h->ev1));
+  CU(h, cudaEventElapsedTime(ms_out, h->ev0, h->ev1));
+  return SGNS_OK;
+}
+
+sgns_status run_plain(sgns_handle* h, int workers, float* ms_out) {
+  const sgns_options& o = h->opt;
+  const size_t stride = plain_worker_bytes(o.size, o.window, o.negative, h->lmax);
+  const size_t need = stride * (size_t)workers;
+  if (need > h->plain_bytes) {
+    dfree(h->plain_scratch);
+    h->plain_bytes = 0;
+    CU(h, cudaMalloc(&h->plain_scratch, need));
+    h->plain_bytes = need;
+  }
+  TrainParams p = make_params(h, workers);
+  p.plain_state = h->plain_scratch;
+  p.plain_stride = (int64_t)stride;
+  sgns_status st = reset_counters(h, workers);
+  if (st) return st;
+  CU(h, cudaEventRecord(h->ev0, h->stream));
+  CU(h, launch_plain_init(p, h->stream));
+  for (int64_t it = 0;; it++) {
+    CU(h, launch_plain_step(p, h->stream));
+    if (it % 64 == 63) {
+      CU(h, cudaMemcpyAsync(&h->h_ctr->active, &h->d_ctr->active, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                            h->stream));
+      CU(h, cudaStreamSynchronize(h->stream));
+      if (h->h_ctr->active <= 0) break;
+    }
+  }
+  CU(h, cudaEventRecord(h->ev1, h->stream));
+  CU(h, cudaEventSynchronize(h->ev1));
+  CU(h, cudaEventElapsedTime(ms_out, h->ev0, h->ev1));
+  return SGNS_OK;
+}
+
+// Autotuner: times each CTA shape of the persistent engine on a prefix of the corpus,
+// on scratch copies of the tables, and keeps the fastest (pairs per second).
+sgns_status autotune(sgns_handle* h) {
+  const sgns_options& o = h->opt;
+  if (o.warps_per_cta > 0) {
+    h->wpc = o.warps_per_cta;
+    h->workers = o.workers;
+    if (!h->workers) {
+      sgns_status st = persistent_shape(h, h->wpc, &h->workers);
+      if (st) return st;
+    }
+    h->tuned = true;
+    return SGNS_OK;
+  }
+  const size_t tbytes = (size_t)h->V * o.size * elem_bytes(o);
+  void *wih_s = nullptr, *woh_s = nullptr;
+  CU(h, cudaMalloc(&wih_s, tbytes));
+  CU(h, cudaMalloc(&woh_s, tbytes));
+  CU(h, cudaMemcpyAsync(wih_s, h->wih, tbytes, cudaMemcpyDeviceToDevice, h->stream));
+  CU(h, cudaMemcpyAsync(woh_s, h->woh, tbytes, cudaMemcpyDeviceToDevice, h->stream));
+  void *wih0 = h->wih, *woh0 = h->woh;
+  const int64_t n0 = h->n_tokens;
+  const int iter0 = h->opt.iter;
+  h->wih = wih_s;
+  h->woh = woh_s;
+  h->opt.iter = 1;
+  double best = -1.0;
+  int best_wpc = 1, best_workers = 0;
+  sgns_status st = SGNS_OK;
+  for (int wpc : {1, 2, 4, 8}) {
+    int workers = 0;
+    st = persistent_shape(h, wpc, &workers);
+    if (st) {
+      st = SGNS_OK;
+      continue;
+    }
+    if (o.workers > 0) workers = o.workers;
+    // a prefix long enough to give every worker a few hundred steps
+    h->n_tokens = std::min<int64_t>(n0, (int64_t)workers * 2000);
+    float ms = 0.f;
+    st = run_persistent(h, workers, wpc, false, &ms);
+    if (st) break;
+    CU(h, cudaMemcpy(h->h_ctr, h->d_ctr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost));
+    const double rate = ms > 0 ? (double)h->h_ctr->pairs / ms : 0.0;
+    if (rate > best) {
+      best = rate;
+      best_wpc = wpc;
+      best_workers = workers;
+    }
+  }
+  h->wih = wih0;
+  h->woh = woh0;
+  h->n_tokens = n0;
+  h->opt.iter = iter0;
+  cudaFree(wih_s);
+  cudaFree(woh_s);
+  if (st) return st;
+  if (best_workers == 0) return fail(h, SGNS_EINVAL, "no persistent-engine shape fits this configuration");
+  h->wpc = best_wpc;
+  h->workers = best_workers;
+  h->tuned = true;
+  if (o.debug > 0)
+    fprintf(stderr, "sgns: autotuned persistent engine: %d warps/CTA, %d workers\n", h->wpc, h->workers);
+  return SGNS_OK;
+}
+
+// Scratch of the kernel-level entry points, one growable buffer per device.
+struct DeviceScratch {
+  std::mutex mx;
+  void* buf = nullptr;
+  size_t bytes = 0;
+  float* exp = nullptr;
+  sgns_status ensure(size_t need) {
+    if (!exp) {
+      float et[kExpTableSize + 1];
+      build_exp_table(et);
+      if (cudaMalloc(&exp, sizeof et) != cudaSuccess) return fail(nullptr, SGNS_ENOMEM, "cudaMalloc");
+      if (cudaMemcpy(exp, et, sizeof et, cudaMemcpyHostToDevice) != cudaSuccess)
+        return fail(nullptr, SGNS_ECUDA, "cudaMemcpy");
+    }
+    if (need <= bytes) return SGNS_OK;
+    if (buf) {
+      cudaDeviceSynchronize();
+      cudaFree(buf);
+    }
+    buf = nullptr;
+    bytes = 0;
+    if (cudaMalloc(&buf, need) != cudaSuccess) return fail(nullptr, SGNS_ENOMEM, "scratch of %zu bytes", need);
+    bytes = need;
+    return SGNS_OK;
+  }
+};
+
+DeviceScratch* device_scratch() {
+  static DeviceScratch table[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  return &table[dev];
+}
+
+}  // namespace
+
+// ===================================================================================
+extern "C" {
+
+void sgns_default_options(sgns_options* o) {
+  std::memset(o, 0, sizeof *o);
+  o->size = 100;  // dsgl.hpp:70
+  o->window = 5;  // dsgl.hpp:69
+  o->negative = 5;
+  o->batch_size = 11;
+  o->sample = 1e-3f;  // dsgl.hpp:75
+  o->alpha = 0.1f;
+  o->min_count = 5;
+  o->iter = 5;
+  o->threads = 12;
+  o->debug = 2;
+  o->binary = 0;
+  o->storage = SGNS_STORE_FP32;
+  o->engine = SGNS_ENGINE_PERSISTENT;
+  o->table_size = 100000000;  // dsgl.hpp:82
+  o->seed = 0x5EEDULL;
+}
+
+sgns_status sgns_options_from_args(sgns_options* o, int argc, const char* const* argv) {
+  auto pos = [&](const char* f) {  // ArgPos, dsgl.hpp:1429-1441
+    for (int a = 1; a < argc; a++)
+      if (!std::strcmp(f, argv[a])) return a;
+    return -1;
+  };
+  struct IntFlag {
+    const char* name;
+    int32_t* dst;
+  } ints[] = {{"-size", &o->size},         {"-debug", &o->debug},         {"-binary", &o->binary},
+              {"-window", &o->window},     {"-negative", &o->negative},   {"-threads", &o->threads},
+              {"-iter", &o->iter},         {"-min-count", &o->min_count}, {"-batch-size", &o->batch_size},
+              {"-workers", &o->workers},   {"-warps-per-cta", &o->warps_per_cta}, {"-device", &o->device},
+              {"-loss", &o->compute_loss}};
+  for (auto& f : ints) {
+    int i = pos(f.name);
+    if (i > 0) {
+      if (i + 1 >= argc) return fail(nullptr, SGNS_EINVAL, "flag %s needs a value", f.name);
+      *f.dst = atoi(argv[i + 1]);
+    }
+  }
+  int i;
+  if ((i = pos("-alpha")) > 0) {
+    if (i + 1 >= argc) return fail(nullptr, SGNS_EINVAL, "flag -alpha needs a value");
+    o->alpha = (float)atof(argv[i + 1]);
+  }
+  if ((i = pos("-sample")) > 0) {
+    if (i + 1 >= argc) return fail(nullptr, SGNS_EINVAL, "flag -sample needs a value");
+    o->sample = (float)atof(argv[i + 1]);
+  }
+  if ((i = pos("-table-size")) > 0) {
+    if (i + 1 >= argc) return fail(nullptr, SGNS_EINVAL, "flag -table-size needs a value");
+    o->table_size = atoll(argv[i + 1]);
+  }
+  if ((i = pos("-seed")) > 0) {
+    if (i + 1 >= argc) return fail(nullptr, SGNS_EINVAL, "flag -seed needs a value");
+    o->seed = strtoull(argv[i + 1], nullptr, 0);
+  }
+  if ((i = pos("-storage")) > 0) {
+    if (i + 1 >= argc) return fail(nullptr, SGNS_EINVAL, "flag -storage needs a value");
+    if (!std::strcmp(argv[i + 1], "fp32")) o->storage = SGNS_STORE_FP32;
+    else if (!std::strcmp(argv[i + 1], "bf16")) o->storage = SGNS_STORE_BF16_SR;
+    else return fail(nullptr, SGNS_EINVAL, "-storage %s: expected fp32 or bf16", argv[i + 1]);
+  }
+  if ((i = pos("-engine")) > 0) {
+    if (i + 1 >= argc) return fail(nullptr, SGNS_EINVAL, "flag -engine needs a value");
+    if (!std::strcmp(argv[i + 1], "plain")) o->engine = SGNS_ENGINE_PLAIN;
+    else if (!std::strcmp(argv[i + 1], "persistent")) o->engine = SGNS_ENGINE_PERSISTENT;
+    else return fail(nullptr, SGNS_EINVAL, "-engine %s: expected plain or persistent", argv[i + 1]);
+  }
+  return SGNS_OK;
+}
+
+sgns_status sgns_create(const sgns_options* opt, sgns_handle** out) {
+  if (!opt || !out) return fail(nullptr, SGNS_EINVAL, "null argument");
+  *out = nullptr;
+  sgns_status st = validate(nullptr, *opt);
+  if (st) return st;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0)
+    return fail(nullptr, SGNS_ECUDA, "no CUDA device available");
+  if (opt->device < 0 || opt->device >= ndev) return fail(nullptr, SGNS_EINVAL, "device %d not present", opt->device);
+  if (cudaSetDevice(opt->device) != cudaSuccess) return fail(nullptr, SGNS_ECUDA, "cudaSetDevice failed");
+  sgns_handle* h = new (std::nothrow) sgns_handle();
+  if (!h) return fail(nullptr, SGNS_ENOMEM, "out of host memory");
+  h->opt = *opt;
+  auto bail = [&](const char* what, cudaError_t e) {
+    fail(nullptr, SGNS_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+    sgns_destroy(h);
+    return SGNS_ECUDA;
+  };
+  cudaError_t e;
+  if ((e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, opt->device)) != cudaSuccess)
+    return bail("cudaDeviceGetAttribute", e);
+  if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess)
+    return bail("cudaStreamCreate", e);
+  if ((e = cudaEventCreate(&h->ev0)) != cudaSuccess || (e = cudaEventCreate(&h->ev1)) != cudaSuccess)
+    return bail("cudaEventCreate", e);
+  if ((e = cudaMalloc(&h->d_ctr, sizeof(DeviceCounters))) != cudaSuccess) return bail("cudaMalloc", e);
+  if ((e = cudaMallocHost(&h->h_ctr, sizeof(DeviceCounters))) != cudaSuccess) return bail("cudaMallocHost", e);
+  if ((e = cudaMalloc(&h->d_flags, 4 * sizeof(int32_t))) != cudaSuccess) return bail("cudaMalloc", e);
+  if ((e = cudaMallocHost(&h->h_flags, 4 * sizeof(int32_t))) != cudaSuccess) return bail("cudaMallocHost", e);
+  if ((e = cudaMalloc(&h->d_exp, sizeof(float) * (kExpTableSize + 1))) != cudaSuccess) return bail("cudaMalloc", e);
+  if ((e = cudaMalloc(&h->d_jumps, sizeof(LcgJumps))) != cudaSuccess) return bail("cudaMalloc", e);
+  float et[kExpTableSize + 1];
+  build_exp_table(et);
+  LcgJumps J;
+  make_lcg_jumps(&J);
+  if ((e = cudaMemcpy(h->d_exp, et, sizeof et, cudaMemcpyHostToDevice)) != cudaSuccess) return bail("cudaMemcpy", e);
+  if ((e = cudaMemcpy(h->d_jumps, &J, sizeof J, cudaMemcpyHostToDevice)) != cudaSuccess) return bail("cudaMemcpy", e);
+  *out = h;
+  return SGNS_OK;
+}
+
+void sgns_destroy(sgns_handle* h) {
+  if (!h) return;
+  cudaSetDevice(h->opt.device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  dfree(h->wih);
+  dfree(h->woh);
+  dfree(h->d_row_of);
+  dfree(h->d_ran);
+  dfree(h->d_table);
+  dfree(h->d_exp);
+  dfree(h->d_jumps);
+  dfree(h->d_ctr);
+  dfree(h->d_flags);
+  dfree(h->d_ids);
+  dfree(h->d_corpus);
+  dfree(h->plain_scratch);
+  if (h->h_ctr) cudaFreeHost(h->h_ctr);
+  if (h->h_flags) cudaFreeHost(h->h_flags);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+const char* sgns_last_error(const sgns_handle* h) {
+  if (h) return h->err.c_str();
+  std::lock_guard<std::mutex> g(g_create_err_mx);
+  return g_create_err.c_str();
+}
+
+sgns_status sgns_set_vocab(sgns_handle* h, const int32_t* counts, int64_t V) {
+  if (!h || !counts) return fail(h, SGNS_EINVAL, "null argument");
+  if (V < 2 || V > (int64_t)INT32_MAX) return fail(h, SGNS_EINVAL, "vocabulary size %lld out of range", (long long)V);
+  CU(h, cudaSetDevice(h->opt.device));
+  for (int64_t i = 0; i < V; i++)
+    if (counts[i] < 0) return fail(h, SGNS_EINVAL, "negative count at vertex %lld", (long long)i);
+  // dsgl.hpp:314-382 and :246-252 -- rows sorted by count, descending (std::sort)
+  std::vector<VocabVertex> v(V);
+  uint64_t tw = 0;
+  for (int64_t i = 0; i < V; i++) {
+    v[i].cn = counts[i];
+    v[i].id = (uint32_t)i;
+    tw += (uint64_t)counts[i];
+  }
+  std::sort(v.begin(), v.end(), [](VocabVertex a, VocabVertex b) { return a.cn > b.cn; });
+  h->V = V;
+  h->train_words = tw;
+  h->order.resize(V);
+  h->row_of.resize(V);
+  h->cn_sorted.resize(V);
+  for (int64_t r = 0; r < V; r++) {
+    h->order[r] = v[r].id;
+    h->row_of[v[r].id] = (int32_t)r;
+    h->cn_sorted[r] = v[r].cn;
+  }
+  std::vector<int32_t> table;
+  build_unigram_table(h->cn_sorted, h->opt.table_size, h->opt.threads, table);
+  // subsampling keep threshold (dsgl.hpp:923-924), indexed by sorted row as the reference
+  // indexes its vertex-indexed count array
+  std::vector<float> ran(V);
+  const float st = h->opt.sample * (float)tw;
+  for (int64_t w = 0; w < V; w++) {
+    const float ratio = st / (float)counts[w];
+    ran[w] = sqrtf(ratio) + ratio;
+  }
+  if (h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  h->tuned = false;
+  dfree(h->wih);
+  dfree(h->woh);
+  dfree(h->d_row_of);
+  dfree(h->d_ran);
+  dfree(h->d_table);
+  dfree(h->d_corpus);
+  dfree(h->d_ids);
+  h->n_tokens = h->corpus_cap = 0;
+  const size_t tbytes = (size_t)V * h->opt.size * elem_bytes(h->opt);
+  cudaError_t e;
+  if ((e = cudaMalloc(&h->wih, tbytes)) != cudaSuccess || (e = cudaMalloc(&h->woh, tbytes)) != cudaSuccess)
+    return fail(h, SGNS_ENOMEM, "embedding tables (2 x %zu bytes): %s", tbytes, cudaGetErrorString(e));
+  CU(h, cudaMalloc(&h->d_row_of, sizeof(int32_t) * V));
+  CU(h, cudaMalloc(&h->d_ran, sizeof(float) * V));
+  CU(h, cudaMalloc(&h->d_table, sizeof(int32_t) * table.size()));
+  CU(h, cudaMemcpy(h->d_row_of, h->row_of.data(), sizeof(int32_t) * V, cudaMemcpyHostToDevice));
+  CU(h, cudaMemcpy(h->d_ran, ran.data(), sizeof(float) * V, cudaMemcpyHostToDevice));
+  CU(h, cudaMemcpy(h->d_table, table.data(), sizeof(int32_t) * table.size(), cudaMemcpyHostToDevice));
+  return sgns_reset_model(h);
+}
+
+sgns_status sgns_reset_model(sgns_handle* h) {
+  if (!h) return fail(h, SGNS_EINVAL, "null handle");
+  if (!h->wih) return fail(h, SGNS_ESTATE, "sgns_set_vocab has not been called");
+  CU(h, cudaSetDevice(h->opt.device));
+  const size_t tbytes = (size_t)h->V * h->opt.size * elem_bytes(h->opt);
+  CU(h, launch_init_wih(h->wih, h->opt.storage == SGNS_STORE_BF16_SR ? STORE_BF16 : STORE_F32, h->V,
+                        h->opt.size, h->d_jumps, h->stream));
+  CU(h, cudaMemsetAsync(h->woh, 0, tbytes, h->stream));
+  CU(h, cudaStreamSynchronize(h->stream));
+  return SGNS_OK;
+}
+
+sgns_status sgns_upload_corpus(sgns_handle* h, const int32_t* tokens, int64_t n) {
+  if (!h || (!tokens && n > 0) || n < 0) return fail(h, SGNS_EINVAL, "bad corpus arguments");
+  if (!h->wih) return fail(h, SGNS_ESTATE, "sgns_set_vocab has not been called");
+  CU(h, cudaSetDevice(h->opt.device));
+  if (n > h->corpus_cap) {
+    dfree(h->d_ids);
+    dfree(h->d_corpus);
+    h->corpus_cap = 0;
+    cudaError_t e;
+    if ((e = cudaMalloc(&h->d_ids, sizeof(int32_t) * n)) != cudaSuccess ||
+        (e = cudaMalloc(&h->d_corpus, sizeof(int32_t) * n)) != cudaSuccess)
+      return fail(h, SGNS_ENOMEM, "corpus of %lld tokens: %s", (long long)n, cudaGetErrorString(e));
+    h->corpus_cap = n;
+  }
+  h->n_tokens = n;
+  CU(h, cudaMemsetAsync(h->d_flags, 0, 4 * sizeof(int32_t), h->stream));
+  if (n > 0) {
+    CU(h, cudaMemcpyAsync(h->d_ids, tokens, sizeof(int32_t) * n, cudaMemcpyHostToDevice, h->stream));
+    CU(h, launch_map_corpus(h->d_ids, h->d_row_of, h->d_corpus, n, h->V, h->d_flags, h->stream));
+    CU(h, launch_max_walk(h->d_corpus, n, h->d_flags + 1, h->stream));
+  }
+  CU(h, cudaMemcpyAsync(h->h_flags, h->d_flags, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+  CU(h, cudaStreamSynchronize(h->stream));
+  if (h->h_flags[0]) {
+    h->n_tokens = 0;
+    return fail(h, SGNS_EINVAL, "corpus holds a token outside [0, %lld) that is not the -1 separator", (long long)h->V);
+  }
+  const int lmax = std::max(2, (int)h->h_flags[1]);
+  if (lmax != h->lmax) h->tuned = false;
+  h->lmax = lmax;
+  return SGNS_OK;
+}
+
+sgns_status sgns_train(sgns_handle* h) {
+  if (!h) return fail(h, SGNS_EINVAL, "null handle");
+  if (!h->wih) return fail(h, SGNS_ESTATE, "sgns_set_vocab has not been called");
+  CU(h, cudaSetDevice(h->opt.device));
+  float ms = 0.f;
+  int workers = 0;
+  sgns_status st;
+  if (h->opt.engine == SGNS_ENGINE_PERSISTENT) {
+    if (!h->tuned) {
+      st = autotune(h);
+      if (st) return st;
+    }
+    workers = h->opt.workers > 0 ? h->opt.workers : h->workers;
+    st = run_persistent(h, workers, h->wpc, true, &ms);
+  } else {
+    workers = h->opt.workers > 0 ? h->opt.workers : h->num_sms * 16;
+    const size_t stride = plain_worker_bytes(h->opt.size, h->opt.window, h->opt.negative, h->lmax);
+    const size_t budget = (size_t)8 << 30;  // HBM set aside for per-worker buffers
+    if (h->opt.workers == 0 && stride * (size_t)workers > budget) workers = std::max<int>(1, (int)(budget / stride));
+    st = run_plain(h, workers, &ms);
+  }
+  if (st) return st;
+  return finish_stats(h, workers, ms);
+}
+
+sgns_status sgns_train_corpus(sgns_handle* h, const int32_t* tokens, int64_t n) {
+  sgns_status st = sgns_upload_corpus(h, tokens, n);
+  if (st) return st;
+  return sgns_train(h);
+}
+
+sgns_status sgns_get_stats(const sgns_handle* h, sgns_stats* out) {
+  if (!h || !out) return SGNS_EINVAL;
+  *out = h->stats;
+  return SGNS_OK;
+}
+
+int64_t sgns_vocab_size(const sgns_handle* h) { return h ? h->V : 0; }
+
+sgns_status sgns_get_order(const sgns_handle* h, uint32_t* out) {
+  if (!h || !out) return SGNS_EINVAL;
+  if (!h->V) return SGNS_ESTATE;
+  std::memcpy(out, h->order.data(), sizeof(uint32_t) * h->V);
+  return SGNS_OK;
+}
+
+sgns_status sgns_get_embeddings(sgns_handle* h, int32_t which, float* out) {
+  if (!h || !out || (which != 0 && which != 1)) return fail(h, SGNS_EINVAL, "bad arguments");
+  if (!h->wih) return fail(h, SGNS_ESTATE, "sgns_set_vocab has not been called");
+  CU(h, cudaSetDevice(h->opt.device));
+  const size_t n = (size_t)h->V * h->opt.size;
+  const void* src = which ? h->woh : h->wih;
+  if (h->opt.storage == SGNS_STORE_BF16_SR) {
+    std::vector<uint16_t> tmp(n);
+    CU(h, cudaMemcpyAsync(tmp.data(), src, n * 2, cudaMemcpyDeviceToHost, h->stream));
+    CU(h, cudaStreamSynchronize(h->stream));
+    for (size_t i = 0; i < n; i++) out[i] = bf16_bits_to_f32(tmp[i]);
+  } else {
+    CU(h, cudaMemcpyAsync(out, src, n * 4, cudaMemcpyDeviceToHost, h->stream));
+    CU(h, cudaStreamSynchronize(h->stream));
+  }
+  return SGNS_OK;
+}
+
+sgns_status sgns_set_embeddings(sgns_handle* h, int32_t which, const float* in) {
+  if (!h || !in || (which != 0 && which != 1)) return fail(h, SGNS_EINVAL, "bad arguments");
+  if (!h->wih) return fail(h, SGNS_ESTATE, "sgns_set_vocab has not been called");
+  CU(h, cudaSetDevice(h->opt.device));
+  const size_t n = (size_t)h->V * h->opt.size;
+  void* dst = which ? h->woh : h->wih;
+  if (h->opt.storage == SGNS_STORE_BF16_SR) {
+    std::vector<uint16_t> tmp(n);
+    for (size_t i = 0; i < n; i++) {  // round to nearest even
+      uint32_t u;
+      std::memcpy(&u, &in[i], 4);
+      if ((u & 0x7F800000u) == 0x7F800000u) tmp[i] = (uint16_t)((u >> 16) | ((u & 0xFFFF) ? 0x40 : 0));
+      else tmp[i] = (uint16_t)((u + 0x7FFFu + ((u >> 16) & 1u)) >> 16);
+    }
+    CU(h, cudaMemcpy(dst, tmp.data(), n * 2, cudaMemcpyHostToDevice));
+  } else {
+    CU(h, cudaMemcpy(dst, in, n * 4, cudaMemcpyHostToDevice));
+  }
+  return SGNS_OK;
+}
+
+sgns_status sgns_device_tables(sgns_handle* h, void** wih, void** woh) {
+  if (!h) return SGNS_EINVAL;
+  if (!h->wih) return fail(h, SGNS_ESTATE, "sgns_set_vocab has not been called");
+  if (wih) *wih = h->wih;
+  if (woh) *woh = h->woh;
+  return SGNS_OK;
+}
+
+sgns_status sgns_save_text(sgns_handle* h, const char* path) {
+  if (!h || !path) return fail(h, SGNS_EINVAL, "bad arguments");
+  if (!h->wih) return fail(h, SGNS_ESTATE, "sgns_set_vocab has not been called");
+  const int64_t V = h->V;
+  const int d = h->opt.size;
+  std::vector<float> w((size_t)V * d);
+  sgns_status st = sgns_get_embeddings(h, 0, w.data());
+  if (st) return st;
+  FILE* f = fopen(path, "wb");
+  if (!f) return fail(h, SGNS_EIO, "cannot open %s for writing", path);
+  fprintf(f, "%lld %lld\n", (long long)V, (long long)d);  // dsgl.hpp:1448
+  // rows formatted in parallel chunks, written in order (dsgl.hpp:1449-1459)
+  const int nth = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+  const int64_t chunk = 4096;
+  bool ok = true;
+  for (int64_t r0 = 0; r0 < V && ok; r0 += chunk * nth) {
+    std::vector<std::string> parts(nth);
+    std::vector<std::thread> th;
+    for (int t = 0; t < nth; t++)
+      th.emplace_back([&, t] {
+        const int64_t lo = r0 + t * chunk, hi = std::min<int64_t>(V, lo + chunk);
+        std::string& s = parts[t];
+        char buf[64];
+        for (int64_t r = lo; r < hi; r++) {
+          int n = snprintf(buf, sizeof buf, "%u ", h->order[r]);
+          s.append(buf, n);
+          if (h->opt.binary) {
+            s.append(reinterpret_cast<const char*>(&w[(size_t)r * d]), sizeof(float) * d);
+          } else {
+            for (int c = 0; c < d; c++) {
+              n = snprintf(buf, sizeof buf, "%f ", w[(size_t)r * d + c]);
+              s.append(buf, n);
+            }
+          }
+          s.push_back('\n');
+        }
+      });
+    for (auto& t : th) t.join();
+    for (auto& s : parts)
+      if (!s.empty() && fwrite(s.data(), 1, s.size(), f) != s.size()) ok = false;
+  }
+  if (fclose(f) != 0) ok = false;
+  if (!ok) return fail(h, SGNS_EIO, "write to %s failed", path);
+  return SGNS_OK;
+}
+
+sgns_status sgns_train_walk_files(sgns_handle* h, const char* const* paths, int32_t n_paths, int64_t V) {
+  if (!h || !paths || n_paths <= 0) return fail(h, SGNS_EINVAL, "bad arguments");
+  std::vector<int32_t> tokens;
+  int64_t max_id = -1;
+  for (int p = 0; p < n_paths; p++) {
+    FILE* f = fopen(paths[p], "rb");
+    if (!f) return fail(h, SGNS_EIO, "cannot open walk file %s", paths[p]);
+    std::vector<char> buf(1 << 22);
+    int64_t cur = -1;  // value being parsed, -1 = none
+    bool line_has_tokens = false;
+    size_t got;
+    while ((got = fread(buf.data(), 1, buf.size(), f)) > 0) {
+      for (size_t i = 0; i < got; i++) {
+        const char c = buf[i];
+        if (c >= '0' && c <= '9') {
+          cur = (cur < 0 ? 0 : cur * 10) + (c - '0');
+          if (cur > INT32_MAX) {
+            fclose(f);
+            return fail(h, SGNS_EINVAL, "vertex id too large in %s", paths[p]);
+          }
+        } else if (c == ' ' || c == '\t' || c == '\r' || c == '\n') {
+          if (cur >= 0) {
+            tokens.push_back((int32_t)cur);
+            max_id = std::max(max_id, cur);
+            line_has_tokens = true;
+            cur = -1;
+          }
+          if (c == '\n' && line_has_tokens) {  // one walk per line (path.hpp:108-110)
+            tokens.push_back(-1);
+            line_has_tokens = false;
+          }
+        } else {
+          fclose(f);
+          return fail(h, SGNS_EINVAL, "unexpected byte 0x%02x in walk file %s", (unsigned char)c, paths[p]);
+        }
+      }
+    }
+    fclose(f);
+    if (cur >= 0) {
+      tokens.push_back((int32_t)cur);
+      max_id = std::max(max_id, cur);
+      line_has_tokens = true;
+    }
+    if (line_has_tokens) tokens.push_back(-1);
+  }
+  if (V <= 0) V = max_id + 1;
+  if (max_id >= V) return fail(h, SGNS_EINVAL, "walk files name vertex %lld >= V = %lld", (long long)max_id, (long long)V);
+  std::vector<int32_t> counts(V, 0);  // vertex_cn, path.hpp:98
+  for (int32_t t : tokens)
+    if (t >= 0) counts[t]++;
+  sgns_status st = sgns_set_vocab(h, counts.data(), V);
+  if (st) return st;
+  return sgns_train_corpus(h, tokens.data(), (int64_t)tokens.size());
+}
+
+sgns_status sgns_minibatch_update(int32_t d, int32_t n, const int32_t* in_count, const int32_t* in_first,
+                                  const int32_t* out_count, const int32_t* out_meta, const float* alpha,
+                                  const float* in_rows, const float* out_rows, float* d_in, float* d_out,
+                                  void* stream) {
+  if (d < 4 || d > kDMax || d % 4 || n < 0) return fail(nullptr, SGNS_EINVAL, "bad minibatch arguments");
+  if (n == 0) return SGNS_OK;
+  DeviceScratch* ds = device_scratch();
+  if (!ds) return fail(nullptr, SGNS_ECUDA, "no current CUDA device");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  std::lock_guard<std::mutex> g(ds->mx);
+  sgns_status st = ds->ensure(sizeof(int64_t) * 2 * n + 16);
+  if (st) return st;
+  int32_t* status = reinterpret_cast<int32_t*>(static_cast<char*>(ds->buf) + sizeof(int64_t) * 2 * n);
+  if (cudaMemsetAsync(status, 0, sizeof(int32_t), s) != cudaSuccess) return fail(nullptr, SGNS_ECUDA, "memset");
+  cudaError_t e = launch_minibatch(d, n, kIMax, kOMax, in_count, in_first, out_count, out_meta, alpha, in_rows,
+                                   out_rows, d_in, d_out, ds->exp, static_cast<int64_t*>(ds->buf), status, s);
+  if (e != cudaSuccess) return fail(nullptr, SGNS_ECUDA, "minibatch kernel: %s", cudaGetErrorString(e));
+  int32_t hs = 0;
+  if ((e = cudaMemcpyAsync(&hs, status, sizeof hs, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    return fail(nullptr, SGNS_ECUDA, "minibatch kernel: %s", cudaGetErrorString(e));
+  if (hs) return fail(nullptr, SGNS_EINVAL, "a minibatch exceeds %d inputs / %d outputs or has first > inputs", kIMax, kOMax);
+  return SGNS_OK;
+}
+
+sgns_status sgns_loss_adjoint(int32_t dtype, int32_t d, int64_t V, int32_t n, const int32_t* in_ptr,
+                              const int32_t* in_ids, const int32_t* in_first, const int32_t* out_ptr,
+                              const int32_t* out_ids, const int32_t* out_meta, const void* wih, const void* woh,
+                              double* loss, int32_t* grad_in_ids, void* grad_in, int64_t* n_in,
+                              int32_t* grad_out_ids, void* grad_out, int64_t* n_out, void* stream) {
+  if (dtype < 0 || dtype > 2 || d < 1 || d > kDMax || V < 1 || V > INT32_MAX || n < 0 || !n_in || !n_out)
+    return fail(nullptr, SGNS_EINVAL, "bad adjoint arguments");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // minibatch extents (host copies of the two offset arrays)
+  std::vector<int32_t> ip(n + 1), op(n + 1);
+  cudaError_t e;
+  if ((e = cudaMemcpyAsync(ip.data(), in_ptr, sizeof(int32_t) * (n + 1), cudaMemcpyDeviceToHost, s)) ||
+      (e = cudaMemcpyAsync(op.data(), out_ptr, sizeof(int32_t) * (n + 1), cudaMemcpyDeviceToHost, s)) ||
+      (e = cudaStreamSynchronize(s)))
+    return fail(nullptr, SGNS_ECUDA, "adjoint: %s", cudaGetErrorString(e));
+  int imax = 1, omax = 1;
+  for (int b = 0; b < n; b++) {
+    const int I = ip[b + 1] - ip[b], O = op[b + 1] - op[b];
+    if (I < 0 || O < 0) return fail(nullptr, SGNS_EINVAL, "adjoint: offsets not ascending at batch %d", b);
+    imax = std::max(imax, I);
+    omax = std::max(omax, O);
+  }
+  if (imax > kIMax || omax > kOMax)
+    return fail(nullptr, SGNS_EINVAL, "adjoint: a minibatch exceeds %d inputs / %d outputs", kIMax, kOMax);
+  DeviceScratch* ds = device_scratch();
+  if (!ds) return fail(nullptr, SGNS_ECUDA, "no current CUDA device");
+  std::lock_guard<std::mutex> g(ds->mx);
+  sgns_status st = ds->ensure(adjoint_scratch_bytes(V) + 64);
+  if (st) return st;
+  int32_t* nu = reinterpret_cast<int32_t*>(static_cast<char*>(ds->buf) + adjoint_scratch_bytes(V));
+  e = launch_adjoint(dtype, d, n, V, ip[n], op[n], in_ptr, in_ids, in_first, out_ptr, out_ids, out_meta, wih, woh,
+                     loss, grad_in_ids, grad_in, grad_out_ids, grad_out, nu, ds->buf, imax, omax, s);
+  if (e != cudaSuccess) return fail(nullptr, SGNS_ECUDA, "adjoint kernels: %s", cudaGetErrorString(e));
+  int32_t h3[3];
+  if ((e = cudaMemcpyAsync(h3, nu, sizeof h3, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s)))
+    return fail(nullptr, SGNS_ECUDA, "adjoint: %s", cudaGetErrorString(e));
+  if (h3[2]) return fail(nullptr, SGNS_EINVAL, "adjoint: a row id outside [0, %lld)", (long long)V);
+  *n_in = h3[0];
+  *n_out = h3[1];
+  return SGNS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,235 @@
+"""ctypes binding of libsgns.so (include/sgns.h) for tests, benchmarks and scripting.
+
+The trainer itself is C++/CUDA behind the C ABI; this module only marshals arguments.
+Loading fails loudly when the shared library has not been built: there is no fallback.
+"""
+import ctypes
+import os
+import re
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+LIB_PATH = os.path.join(HERE, "build", "libsgns.so")
+HEADER = os.path.join(ROOT, "include", "sgns.h")
+
+OK, EINVAL, ENOMEM, ECUDA, ETIMEOUT, EIO, ESTATE = range(7)
+STORE_FP32, STORE_BF16_SR = 0, 1
+ENGINE_PLAIN, ENGINE_PERSISTENT = 0, 1
+
+
+class Options(ctypes.Structure):
+    _fields_ = [
+        ("size", ctypes.c_int32), ("window", ctypes.c_int32), ("negative", ctypes.c_int32),
+        ("batch_size", ctypes.c_int32), ("sample", ctypes.c_float), ("alpha", ctypes.c_float),
+        ("min_count", ctypes.c_int32), ("iter", ctypes.c_int32), ("threads", ctypes.c_int32),
+        ("debug", ctypes.c_int32), ("binary", ctypes.c_int32), ("storage", ctypes.c_int32),
+        ("engine", ctypes.c_int32), ("workers", ctypes.c_int32), ("warps_per_cta", ctypes.c_int32),
+        ("device", ctypes.c_int32), ("compute_loss", ctypes.c_int32), ("reserved0", ctypes.c_int32),
+        ("table_size", ctypes.c_int64), ("seed", ctypes.c_uint64),
+    ]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [
+        ("steps", ctypes.c_uint64), ("pairs", ctypes.c_uint64), ("word_count_actual", ctypes.c_uint64),
+        ("row_bytes", ctypes.c_uint64), ("loss", ctypes.c_double), ("final_alpha", ctypes.c_float),
+        ("train_ms", ctypes.c_float), ("workers", ctypes.c_int32), ("warps_per_cta", ctypes.c_int32),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class SgnsError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("sgns status %d: %s" % (status, msg))
+        self.status = status
+
+
+_lib = None
+
+
+def header_functions():
+    """Names of the functions include/sgns.h declares."""
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(sgns_[a-z_0-9]+)\s*\(", text)))
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libsgns.so is not built (%s); run __graft_entry__.build()" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        vp, i32, i64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64
+        L.sgns_last_error.restype = ctypes.c_char_p
+        L.sgns_last_error.argtypes = [vp]
+        L.sgns_default_options.argtypes = [ctypes.POINTER(Options)]
+        L.sgns_default_options.restype = None
+        L.sgns_options_from_args.argtypes = [ctypes.POINTER(Options), ctypes.c_int, ctypes.POINTER(ctypes.c_char_p)]
+        L.sgns_create.argtypes = [ctypes.POINTER(Options), ctypes.POINTER(vp)]
+        L.sgns_destroy.argtypes = [vp]
+        L.sgns_destroy.restype = None
+        L.sgns_set_vocab.argtypes = [vp, vp, i64]
+        L.sgns_reset_model.argtypes = [vp]
+        L.sgns_upload_corpus.argtypes = [vp, vp, i64]
+        L.sgns_train.argtypes = [vp]
+        L.sgns_train_corpus.argtypes = [vp, vp, i64]
+        L.sgns_train_walk_files.argtypes = [vp, ctypes.POINTER(ctypes.c_char_p), i32, i64]
+        L.sgns_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+        L.sgns_vocab_size.argtypes = [vp]
+        L.sgns_vocab_size.restype = i64
+        L.sgns_get_order.argtypes = [vp, vp]
+        L.sgns_get_embeddings.argtypes = [vp, i32, vp]
+        L.sgns_set_embeddings.argtypes = [vp, i32, vp]
+        L.sgns_device_tables.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp)]
+        L.sgns_save_text.argtypes = [vp, ctypes.c_char_p]
+        L.sgns_minibatch_update.argtypes = [i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+        L.sgns_loss_adjoint.argtypes = [i32, i32, i64, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp,
+                                        ctypes.POINTER(i64), vp, vp, ctypes.POINTER(i64), vp]
+        for name in header_functions():  # every declared entry point must be exported
+            getattr(L, name)
+        _lib = L
+    return _lib
+
+
+def _check(status, handle=None):
+    if status != OK:
+        msg = lib().sgns_last_error(handle)
+        raise SgnsError(status, msg.decode() if msg else "")
+
+
+def default_options(**kw):
+    o = Options()
+    lib().sgns_default_options(ctypes.byref(o))
+    for k, v in kw.items():
+        if k == "storage" and isinstance(v, str):
+            v = {"fp32": STORE_FP32, "bf16": STORE_BF16_SR}[v]
+        if k == "engine" and isinstance(v, str):
+            v = {"plain": ENGINE_PLAIN, "persistent": ENGINE_PERSISTENT}[v]
+        setattr(o, k, v)
+    return o
+
+
+def options_from_args(args, base=None):
+    o = base if base is not None else default_options()
+    argv = (ctypes.c_char_p * (len(args) + 1))(*([b"prog"] + [a.encode() for a in args]))
+    _check(lib().sgns_options_from_args(ctypes.byref(o), len(args) + 1, argv))
+    return o
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class Trainer:
+    """One sgns_handle: vocabulary, device tables, corpus and training calls."""
+
+    def __init__(self, options=None, **kw):
+        self.opt = options if options is not None else default_options(**kw)
+        h = ctypes.c_void_p()
+        _check(lib().sgns_create(ctypes.byref(self.opt), ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().sgns_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_vocab(self, counts):
+        counts = np.ascontiguousarray(counts, dtype=np.int32)
+        _check(lib().sgns_set_vocab(self.h, _ptr(counts), len(counts)), self.h)
+
+    def reset_model(self):
+        _check(lib().sgns_reset_model(self.h), self.h)
+
+    def upload(self, tokens):
+        tokens = np.ascontiguousarray(tokens, dtype=np.int32)
+        _check(lib().sgns_upload_corpus(self.h, _ptr(tokens), len(tokens)), self.h)
+
+    def train(self):
+        _check(lib().sgns_train(self.h), self.h)
+        return self.stats()
+
+    def train_corpus(self, tokens):
+        """tokens: numpy int32 (host); pinned buffers may be passed as numpy views."""
+        tokens = np.ascontiguousarray(tokens, dtype=np.int32)
+        _check(lib().sgns_train_corpus(self.h, _ptr(tokens), len(tokens)), self.h)
+        return self.stats()
+
+    def train_corpus_ptr(self, ptr, n):
+        _check(lib().sgns_train_corpus(self.h, ctypes.c_void_p(ptr), n), self.h)
+        return self.stats()
+
+    def train_walk_files(self, paths, vertices=0):
+        arr = (ctypes.c_char_p * len(paths))(*[p.encode() for p in paths])
+        _check(lib().sgns_train_walk_files(self.h, arr, len(paths), vertices), self.h)
+        return self.stats()
+
+    def stats(self):
+        s = Stats()
+        _check(lib().sgns_get_stats(self.h, ctypes.byref(s)))
+        return s
+
+    @property
+    def vocab_size(self):
+        return lib().sgns_vocab_size(self.h)
+
+    def order(self):
+        o = np.zeros(self.vocab_size, dtype=np.uint32)
+        _check(lib().sgns_get_order(self.h, _ptr(o)), self.h)
+        return o
+
+    def embeddings(self, which=0):
+        out = np.zeros((self.vocab_size, self.opt.size), dtype=np.float32)
+        _check(lib().sgns_get_embeddings(self.h, which, _ptr(out)), self.h)
+        return out
+
+    def set_embeddings(self, which, values):
+        values = np.ascontiguousarray(values, dtype=np.float32)
+        _check(lib().sgns_set_embeddings(self.h, which, _ptr(values)), self.h)
+
+    def device_tables(self):
+        a, b = ctypes.c_void_p(), ctypes.c_void_p()
+        _check(lib().sgns_device_tables(self.h, ctypes.byref(a), ctypes.byref(b)), self.h)
+        return a.value, b.value
+
+    def save_text(self, path):
+        _check(lib().sgns_save_text(self.h, path.encode()), self.h)
+
+
+def minibatch_update(d, in_count, in_first, out_count, out_meta, alpha, in_rows, out_rows, d_in, d_out,
+                     stream=0):
+    """All array arguments are CUDA torch tensors (device pointers)."""
+    n = int(in_count.numel())
+    _check(lib().sgns_minibatch_update(d, n, in_count.data_ptr(), in_first.data_ptr(), out_count.data_ptr(),
+                                       out_meta.data_ptr(), alpha.data_ptr(), in_rows.data_ptr(),
+                                       out_rows.data_ptr(), d_in.data_ptr(), d_out.data_ptr(),
+                                       ctypes.c_void_p(stream)))
+
+
+def loss_adjoint(dtype, d, V, in_ptr, in_ids, in_first, out_ptr, out_ids, out_meta, wih, woh, loss,
+                 grad_in_ids, grad_in, grad_out_ids, grad_out, stream=0):
+    """Device tensors in, (n_in, n_out) out; fills loss / ids / grads in place."""
+    n = int(in_first.numel())
+    n_in, n_out = ctypes.c_int64(), ctypes.c_int64()
+    _check(lib().sgns_loss_adjoint(dtype, d, V, n, in_ptr.data_ptr(), in_ids.data_ptr(), in_first.data_ptr(),
+                                   out_ptr.data_ptr(), out_ids.data_ptr(), out_meta.data_ptr(), wih, woh,
+                                   loss.data_ptr(), grad_in_ids.data_ptr(), grad_in.data_ptr(),
+                                   ctypes.byref(n_in), grad_out_ids.data_ptr(), grad_out.data_ptr(),
+                                   ctypes.byref(n_out), ctypes.c_void_p(stream)))
+    return n_in.value, n_out.value

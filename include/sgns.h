@@ -1,0 +1,173 @@
+/* sgns.h -- C ABI of the GB300 DSGL skip-gram negative-sampling trainer.
+ *
+ * A drop-in for the trainer DistGER's huge_walk runs over its walk corpus:
+ *   int dsgl(int argc, char** argv, vector<int>* vertex_cn,
+ *            vector<vertex_id_t>* new_sort, WalkEngine<real_t,uint32_t>* graph)
+ *   (include/dsgl.hpp:1464 in trsenli/GDistGER-re; called from the commented-out
+ *   src/examples/huge_walk.cpp:133), and its GPU sibling
+ *   int train_corpus_cuda(int argc, char** argv, ...)  (src/word2vec.cu:1429).
+ * The reference passes everything through argv flags and globals and exits on error;
+ * here a handle owns all device memory, options are a plain struct (filled from the
+ * same flags by sgns_options_from_args), and every call returns an sgns_status.
+ *
+ * Pointers are host pointers unless a parameter says "device".  All entry points are
+ * thread-safe for distinct handles; one handle must not be used by two threads at once.
+ */
+#ifndef SGNS_H_
+#define SGNS_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum sgns_status {
+  SGNS_OK = 0,
+  SGNS_EINVAL = 1,   /* bad argument or option (message in sgns_last_error) */
+  SGNS_ENOMEM = 2,   /* host or device allocation failed */
+  SGNS_ECUDA = 3,    /* CUDA runtime error, or no usable GPU */
+  SGNS_ETIMEOUT = 4, /* a device-side bounded wait gave up */
+  SGNS_EIO = 5,      /* file could not be read or written */
+  SGNS_ESTATE = 6    /* call out of order (e.g. training before sgns_set_vocab) */
+} sgns_status;
+
+typedef enum sgns_storage {
+  SGNS_STORE_FP32 = 0,    /* reference precision */
+  SGNS_STORE_BF16_SR = 1  /* bf16 tables, fp32 arithmetic, stochastic rounding on write-back */
+} sgns_storage;
+
+typedef enum sgns_engine {
+  /* Reference memory policy (per-walk input buffers snapshot at walk load and written
+   * back at walk end; per-pool negative buffer), state in HBM, one launch per step.
+   * With workers = 1 it reproduces the reference's single-thread result bit for bit. */
+  SGNS_ENGINE_PLAIN = 0,
+  /* Persistent kernel: one launch trains the whole corpus; each worker holds its two
+   * walks' context rows in shared memory over the sliding window [pos-w, pos+w] and
+   * reads/updates negative rows in the table directly.  Launch captured in a CUDA
+   * graph; warps per CTA and worker count chosen by the autotuner. */
+  SGNS_ENGINE_PERSISTENT = 1
+} sgns_engine;
+
+typedef struct sgns_options {
+  int32_t size;        /* -size       hidden size d (multiple of 4, <= 256)       */
+  int32_t window;      /* -window     w (1..16)                                   */
+  int32_t negative;    /* -negative   K (0..10)                                   */
+  int32_t batch_size;  /* -batch-size accepted; the reference replaces it by 2w+1 (dsgl.hpp:832) */
+  float sample;        /* -sample     subsampling threshold                       */
+  float alpha;         /* -alpha      starting learning rate (linear decay)       */
+  int32_t min_count;   /* -min-count  accepted; unused by the reference vocab path (dsgl.hpp:314-382) */
+  int32_t iter;        /* -iter       passes over the corpus                      */
+  int32_t threads;     /* -threads    partition of the unigram-table sum (dsgl.hpp:127) */
+  int32_t debug;       /* -debug                                                  */
+  int32_t binary;      /* -binary     1 = raw float rows in sgns_save_text        */
+  int32_t storage;     /* sgns_storage                                            */
+  int32_t engine;      /* sgns_engine                                             */
+  int32_t workers;     /* independent trainers (the reference's compute threads); 0 = tuned */
+  int32_t warps_per_cta; /* persistent engine CTA shape; 0 = tuned                */
+  int32_t device;      /* CUDA device ordinal                                     */
+  int32_t compute_loss;/* 1 = also accumulate the SGNS loss (fp64 reduction)      */
+  int32_t reserved0;
+  int64_t table_size;  /* unigram table entries (the reference fixes 1e8, dsgl.hpp:82) */
+  uint64_t seed;       /* stochastic-rounding stream seed                         */
+} sgns_options;
+
+typedef struct sgns_stats {
+  uint64_t steps;              /* minibatches trained (one per target pair of walks) */
+  uint64_t pairs;              /* (context, target) pairs = input rows over all steps */
+  uint64_t word_count_actual;  /* tokens consumed, as the reference counts them      */
+  uint64_t row_bytes;          /* algorithmic row traffic of the run  */
+  double loss;                 /* sum of SGNS losses (compute_loss = 1), fp64        */
+  float final_alpha;
+  float train_ms;              /* device time of the last training call              */
+  int32_t workers;
+  int32_t warps_per_cta;
+} sgns_stats;
+
+/* Defaults of dsgl.hpp:67-76, table_size 1e8, persistent engine, fp32. */
+void sgns_default_options(sgns_options* opt);
+/* Fills opt from word2vec-style flags exactly as dsgl.hpp:1495-1535 scans them
+ * (unknown flags ignored).  Adds -storage fp32|bf16, -engine plain|persistent,
+ * -workers N, -table-size N, -seed N. */
+sgns_status sgns_options_from_args(sgns_options* opt, int argc, const char* const* argv);
+
+typedef struct sgns_handle sgns_handle;
+
+/* Creates a trainer on opt->device.  Replaces dsgl()'s flag scan and globals. */
+sgns_status sgns_create(const sgns_options* opt, sgns_handle** out);
+void sgns_destroy(sgns_handle* h);
+/* Message of the last failed call on h (or of the last failed sgns_create when h is NULL). */
+const char* sgns_last_error(const sgns_handle* h);
+
+/* Vocabulary from per-vertex occurrence counts (the reference's vertex_cn), then the
+ * reference's set-up: rows sorted by count (dsgl.hpp:246-252, 314-382), the unigram^0.75
+ * table (dsgl.hpp:121-147), Wih from the reference LCG, Woh = 0 (dsgl.hpp:433-457), the
+ * sigmoid table (dsgl.hpp:1557-1562).  Requires V >= 2 (the reference asserts V > 1000). */
+sgns_status sgns_set_vocab(sgns_handle* h, const int32_t* vertex_counts, int64_t V);
+/* Re-initialises Wih/Woh as sgns_set_vocab does, keeping vocabulary and tables. */
+sgns_status sgns_reset_model(sgns_handle* h);
+
+/* Copies a corpus to the device: vertex ids with -1 walk separators, the in-memory
+ * walk stream the reference reads from graph->local_corpus (path.hpp:96,110). */
+sgns_status sgns_upload_corpus(sgns_handle* h, const int32_t* tokens, int64_t n_tokens);
+/* Trains -iter passes over the uploaded corpus (Train_SGNS_MPI, dsgl.hpp:522-1427). */
+sgns_status sgns_train(sgns_handle* h);
+/* Upload + train in one call: the reference's dsgl() hot path from host memory. */
+sgns_status sgns_train_corpus(sgns_handle* h, const int32_t* tokens, int64_t n_tokens);
+/* Reads one or more walk files (" %u" per vertex, one walk per line; path.hpp:92,108),
+ * counts vertices, builds the vocabulary over max_vertex_id+1 vertices (or V if V > 0),
+ * uploads and trains. */
+sgns_status sgns_train_walk_files(sgns_handle* h, const char* const* paths, int32_t n_paths, int64_t V);
+
+sgns_status sgns_get_stats(const sgns_handle* h, sgns_stats* out);
+int64_t sgns_vocab_size(const sgns_handle* h);
+/* Row -> vertex id of the frequency-sorted rows (v_vocab[r].id). */
+sgns_status sgns_get_order(const sgns_handle* h, uint32_t* order_out);
+/* which: 0 = Wih (the written embedding), 1 = Woh.  V*d floats in sorted-row order. */
+sgns_status sgns_get_embeddings(sgns_handle* h, int32_t which, float* out);
+/* Overwrites Wih/Woh (sorted-row order, V*d floats; rounded to nearest for bf16). */
+sgns_status sgns_set_embeddings(sgns_handle* h, int32_t which, const float* in);
+/* Device pointers of Wih/Woh (fp32 or bf16 elements, sorted-row order). */
+sgns_status sgns_device_tables(sgns_handle* h, void** wih, void** woh);
+/* my_saveModel (dsgl.hpp:1443-1461): "V d\n" then "<id> " + d x "%f " + "\n" per row. */
+sgns_status sgns_save_text(sgns_handle* h, const char* path);
+
+/* ---- kernel-level entry points (device pointers, caller's stream) ------------------
+ * One minibatch update of the reference step (dsgl.hpp:1241-1311) for n independent
+ * minibatches whose rows are given explicitly, computed by the same device code as the
+ * trainers.  Per minibatch b: in_count[b] input rows (in_first[b] of them from walk 1),
+ * out_count[b] output rows (row 0 = target of walk 1, last = target of walk 2),
+ * out_meta = multiplicities, alpha[b].  Rows are concatenated over b (fp32).  Writes
+ * d_in (the reference's updated inputM) and d_out (outputMd).  storage selects the
+ * accumulation of the trainer that is mirrored (fp32 for both storages). */
+sgns_status sgns_minibatch_update(int32_t d, int32_t n_batches, const int32_t* in_count,
+                                  const int32_t* in_first, const int32_t* out_count,
+                                  const int32_t* out_meta, const float* alpha,
+                                  const float* in_rows, const float* out_rows, float* d_in,
+                                  float* d_out, void* stream);
+
+/* SGNS loss and its hand-written adjoint for n minibatches that index tables of V
+ * rows (device pointers).  Minibatch b has inputs in_ids[in_ptr[b]..in_ptr[b+1]), the
+ * first in_first[b] of them labelled by output 0 and the rest by the last output, and
+ * outputs out_ids[out_ptr[b]..out_ptr[b+1]) with multiplicities out_meta (the layout of
+ * one reference step, dsgl.hpp:1103-1159).  With f_ij = <Woh[o_i], Wih[x_j]>:
+ *   *loss = sum meta_i * softplus(-(2*label_ij - 1) * f_ij), reduced in fp64 (device);
+ *   grad_in_ids/grad_in: the distinct Wih rows of the batch in ascending order and
+ *   dL/dWih for each (n_in x d); grad_out_ids/grad_out likewise for Woh.
+ * dtype: 0 = fp32 tables and gradients; 1 = bf16 tables, fp32 arithmetic and gradients;
+ * 2 = fp64 tables, arithmetic and gradients.  Id/gradient capacities: in_ptr[n] and
+ * out_ptr[n] rows.  n_in/n_out are host pointers; the call returns once they are known.
+ * A V-sized scratch is allocated by the library and cached per device. */
+sgns_status sgns_loss_adjoint(int32_t dtype, int32_t d, int64_t V, int32_t n_batches,
+                              const int32_t* in_ptr, const int32_t* in_ids,
+                              const int32_t* in_first, const int32_t* out_ptr,
+                              const int32_t* out_ids, const int32_t* out_meta,
+                              const void* wih, const void* woh, double* loss,
+                              int32_t* grad_in_ids, void* grad_in, int64_t* n_in,
+                              int32_t* grad_out_ids, void* grad_out, int64_t* n_out,
+                              void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,122 @@
+"""The C ABI library without a GPU: symbols, option parsing, arithmetic helpers."""
+import random
+import subprocess
+
+import numpy as np
+import pytest
+
+import sgns
+
+
+def test_every_declared_symbol_is_exported(sgns_lib):
+    names = sgns.header_functions()
+    assert len(names) >= 20
+    out = subprocess.run(["nm", "-D", "--defined-only", sgns.LIB_PATH], capture_output=True, text=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if line.strip()}
+    missing = [n for n in names if n not in exported]
+    assert not missing, missing
+
+
+def test_defaults_are_the_references(sgns_lib):
+    o = sgns.default_options()
+    # include/dsgl.hpp:67-76, 82
+    assert (o.size, o.window, o.negative, o.iter, o.threads, o.batch_size, o.min_count) == (100, 5, 5, 5, 12, 11, 5)
+    assert abs(o.alpha - 0.1) < 1e-7 and abs(o.sample - 1e-3) < 1e-9
+    assert o.table_size == 100000000
+
+
+def test_reference_flags_parse(sgns_lib):
+    args = ["-size", "128", "-window", "10", "-negative", "5", "-batch-size", "21", "-sample", "1e-3",
+            "-alpha", "0.01", "-min-count", "0", "-iter", "3", "-threads", "10", "-debug", "2",
+            "-sync-size", "1024", "-storage", "bf16", "-engine", "plain", "-workers", "77"]
+    o = sgns.options_from_args(args)
+    assert (o.size, o.window, o.negative, o.batch_size, o.min_count, o.iter, o.threads) == (128, 10, 5, 21, 0, 3, 10)
+    assert abs(o.alpha - 0.01) < 1e-8
+    assert o.storage == sgns.STORE_BF16_SR and o.engine == sgns.ENGINE_PLAIN and o.workers == 77
+
+
+def test_flag_without_value_is_an_error(sgns_lib):
+    with pytest.raises(sgns.SgnsError) as e:
+        sgns.options_from_args(["-size"])
+    assert e.value.status == sgns.EINVAL
+
+
+def test_bad_storage_name(sgns_lib):
+    with pytest.raises(sgns.SgnsError):
+        sgns.options_from_args(["-storage", "fp8"])
+
+
+def test_invalid_options_rejected_before_device(sgns_lib):
+    for kw in (dict(size=130), dict(size=512), dict(window=0), dict(window=16), dict(negative=11), dict(iter=0)):
+        with pytest.raises(sgns.SgnsError) as e:
+            sgns.Trainer(**kw)
+        assert e.value.status == sgns.EINVAL
+
+
+def test_create_without_gpu_fails_loudly(sgns_lib):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(sgns.SgnsError) as e:
+        sgns.Trainer(size=16)
+    assert e.value.status == sgns.ECUDA
+
+
+# ---- arithmetic the kernels rely on, restated exactly in Python ---------------------
+def gm_magic(d):
+    l = 0
+    while (1 << l) < d:
+        l += 1
+    m = ((1 << 64) * ((1 << l) - d)) // d + 1
+    return m & ((1 << 64) - 1), l - 1
+
+
+def gm_div(n, d):
+    if d == 1:
+        return n
+    m, sh = gm_magic(d)
+    t = (m * n) >> 64
+    return (t + ((n - t) >> 1)) >> sh
+
+
+@pytest.mark.parametrize("d", [2, 3, 5, 7, 10, 1099, 1500, 9999, 10_000_000, 100_000_000, 2_238_730, 3_999_999,
+                               (1 << 31) - 1, (1 << 32) + 15, (1 << 63) + 12345])
+def test_invariant_division(d):
+    rnd = random.Random(d)
+    vals = [0, 1, d - 1, d, d + 1, 2 * d - 1, (1 << 48) - 1, (1 << 64) - 1, (1 << 63)]
+    vals += [rnd.getrandbits(64) for _ in range(2000)] + [rnd.getrandbits(48) for _ in range(2000)]
+    for n in vals:
+        assert gm_div(n, d) == n // d
+
+
+def test_lcg_jump_ahead():
+    A, C, M = 25214903917, 11, (1 << 64) - 1
+    pm, pa = A, C
+    pows = []
+    for _ in range(20):
+        pows.append((pm, pa))
+        pa = (pm * pa + pa) & M
+        pm = (pm * pm) & M
+    r0 = 12345
+    for n in (0, 1, 2, 31, 32, 33, 1000, 65537):
+        r = r0
+        for _ in range(n):
+            r = (r * A + C) & M
+        j, k, i = r0, n, 0
+        while k:
+            if k & 1:
+                j = (pows[i][0] * j + pows[i][1]) & M
+            k >>= 1
+            i += 1
+        assert j == r
+
+
+def test_bf16_stochastic_rounding_is_unbiased():
+    # the rounding rule of the kernels and the oracle: add 16 uniform bits, truncate
+    rng = np.random.default_rng(0)
+    x = np.float32(1.0 + 2 ** -9 * 0.3)
+    u = np.array([x], np.float32).view(np.uint32)[0]
+    r = rng.integers(0, 1 << 16, 200000).astype(np.uint64)
+    v = ((np.uint64(u) + r) >> np.uint64(16)).astype(np.uint32) << 16
+    mean = v.view(np.float32).astype(np.float64).mean()
+    assert abs(mean - float(x)) < 2 ** -9 * 0.01

@@ -1,0 +1,158 @@
+"""GPU trainers against the reference's golden vectors and the oracle.
+
+With one worker the trainers follow the reference's single-compute-thread order, so
+results must be identical bit for bit: the plain engine against the reference policy
+(and the reference's own golden outputs), the persistent engine against the oracle's
+GPU-resident window policy, in fp32 and in bf16 with stochastic rounding."""
+import glob
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+import sgns
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+GOLDEN_CASES = sorted(os.path.basename(p)[:-5] for p in glob.glob(os.path.join(GOLDEN, "*.json")))
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def golden(name):
+    meta = json.load(open(os.path.join(GOLDEN, name + ".json")))
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    return meta, z["corpus"]
+
+
+def synthetic(name):
+    import torch
+    import synth
+
+    if name == "cl_d128":
+        ip, ix = synth.chung_lu(3000, 20000, 2.1, seed=21)
+        c = synth.random_walks(ip, ix, 3, 40, seed=22)
+        return dict(V=3000, d=128, window=10, negative=5, iter=1, sample=1e-3, alpha=0.01), c.numpy()
+    if name == "cl_d256_k10":
+        ip, ix = synth.chung_lu(2000, 12000, 2.1, seed=23)
+        L = synth.walk_lengths(2000 * 2, "geometric", mean=30, cap=80, seed=24)
+        c = synth.random_walks(ip, ix, 2, L, seed=25)
+        return dict(V=2000, d=256, window=5, negative=10, iter=2, sample=1e-3, alpha=0.025), c.numpy()
+    if name == "sbm_d64_w15":
+        ip, ix, _ = synth.sbm(2400, 12000, seed=26)
+        L = synth.walk_lengths(2400 * 2, "uniform", lo=5, hi=120, seed=27)
+        c = synth.random_walks(ip, ix, 2, L, seed=28)
+        return dict(V=2400, d=64, window=15, negative=3, iter=1, sample=1e-4, alpha=0.02), c.numpy()
+    raise KeyError(name)
+
+
+ALL_CASES = GOLDEN_CASES + ["cl_d128", "cl_d256_k10", "sbm_d64_w15"]
+
+
+def case(name):
+    if name in GOLDEN_CASES:
+        meta, corpus = golden(name)
+        cfg = {k: meta[k] for k in ("V", "d", "window", "negative", "iter", "sample", "alpha")}
+        return cfg, corpus, meta
+    cfg, corpus = synthetic(name)
+    return cfg, corpus.astype(np.int32), None
+
+
+def gpu_train(cfg, corpus, engine, storage, workers=1, wpc=1, table_size=None, table_threads=2):
+    counts = np.bincount(corpus[corpus >= 0], minlength=cfg["V"]).astype(np.int32)
+    opt = sgns.default_options(size=cfg["d"], window=cfg["window"], negative=cfg["negative"], iter=cfg["iter"],
+                               sample=cfg["sample"], alpha=cfg["alpha"], engine=engine, storage=storage,
+                               workers=workers, warps_per_cta=wpc, threads=table_threads,
+                               table_size=table_size or 1000000, debug=0)
+    with sgns.Trainer(opt) as t:
+        t.set_vocab(counts)
+        st = t.train_corpus(corpus)
+        return t.embeddings(0), t.embeddings(1), st, t.order()
+
+
+def oracle_train(oracle_mod, cfg, corpus, policy, storage, workers=1, table_size=None, table_threads=2):
+    counts = np.bincount(corpus[corpus >= 0], minlength=cfg["V"]).astype(np.int32)
+    st = {"fp32": oracle_mod.STORE_F32, "bf16": oracle_mod.STORE_BF16}[storage]
+    wih, woh, stats = oracle_mod.train(corpus, counts, d=cfg["d"], window=cfg["window"], negative=cfg["negative"],
+                                       iter=cfg["iter"], workers=workers, threads=1, table_threads=table_threads,
+                                       policy=policy, storage=st, table_size=table_size or 1000000,
+                                       sample=cfg["sample"], alpha=cfg["alpha"])
+    if storage == "bf16":
+        wih, woh = oracle_mod.bf16_to_f32(wih), oracle_mod.bf16_to_f32(woh)
+    return wih, woh, stats
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_plain_fp32_reproduces_reference_outputs(name, sgns_lib):
+    cfg, corpus, meta = case(name)
+    wih, woh, st, order = gpu_train(cfg, corpus, "plain", "fp32", table_size=meta["table_size"])
+    assert np.array_equal(order, np.load(os.path.join(GOLDEN, name + ".npz"))["order"])
+    assert sha(wih) == meta["wih_sha256"], np.abs(wih[0] - np.array(meta["wih_row0"], np.float32)).max()
+    assert sha(woh) == meta["woh_sha256"]
+
+
+@pytest.mark.parametrize("storage", ["fp32", "bf16"])
+@pytest.mark.parametrize("name", ALL_CASES)
+def test_plain_matches_oracle(name, storage, sgns_lib, oracle_mod):
+    cfg, corpus, _ = case(name)
+    wih, woh, st, _ = gpu_train(cfg, corpus, "plain", storage)
+    owih, owoh, ost = oracle_train(oracle_mod, cfg, corpus, oracle_mod.POLICY_REF, storage)
+    assert (st.steps, st.pairs, st.word_count_actual) == (ost["steps"], ost["pairs"], ost["word_count_actual"])
+    assert np.array_equal(wih.view(np.uint32), owih.view(np.uint32)), np.abs(wih - owih).max()
+    assert np.array_equal(woh.view(np.uint32), owoh.view(np.uint32)), np.abs(woh - owoh).max()
+
+
+@pytest.mark.parametrize("wpc", [1, 2])
+@pytest.mark.parametrize("storage", ["fp32", "bf16"])
+@pytest.mark.parametrize("name", ALL_CASES)
+def test_persistent_matches_oracle(name, storage, wpc, sgns_lib, oracle_mod):
+    cfg, corpus, _ = case(name)
+    wih, woh, st, _ = gpu_train(cfg, corpus, "persistent", storage, wpc=wpc)
+    owih, owoh, ost = oracle_train(oracle_mod, cfg, corpus, oracle_mod.POLICY_WINDOW, storage)
+    assert (st.steps, st.pairs, st.word_count_actual) == (ost["steps"], ost["pairs"], ost["word_count_actual"])
+    assert abs(st.final_alpha - ost["final_alpha"]) == 0
+    assert np.array_equal(wih.view(np.uint32), owih.view(np.uint32)), np.abs(wih - owih).max()
+    assert np.array_equal(woh.view(np.uint32), owoh.view(np.uint32)), np.abs(woh - owoh).max()
+
+
+@pytest.mark.parametrize("engine,policy", [("plain", 0), ("persistent", 1)])
+def test_many_workers_follow_the_reference_control_flow(engine, policy, sgns_lib, oracle_mod):
+    """Hogwild workers race on table rows, but every worker's control flow (slice,
+    subsampling, windows, negatives, learning-rate schedule inputs) is independent of
+    the table values: step, pair and word counts equal the oracle's exactly."""
+    cfg, corpus, _ = case("cl_d128")
+    W = 37
+    wih, woh, st, _ = gpu_train(cfg, corpus, engine, "fp32", workers=W, wpc=1)
+    owih, owoh, ost = oracle_train(oracle_mod, cfg, corpus, policy, "fp32", workers=W)
+    assert (st.steps, st.pairs, st.word_count_actual) == (ost["steps"], ost["pairs"], ost["word_count_actual"])
+    assert np.isfinite(wih).all() and np.isfinite(woh).all()
+
+
+def test_invalid_vertex_id_is_rejected(sgns_lib):
+    opt = sgns.default_options(size=8, window=2, negative=2, iter=1, debug=0, table_size=1000)
+    with sgns.Trainer(opt) as t:
+        t.set_vocab(np.ones(10, np.int32))
+        with pytest.raises(sgns.SgnsError) as e:
+            t.upload(np.array([1, 2, 10, -1], np.int32))
+        assert e.value.status == sgns.EINVAL
+        with pytest.raises(sgns.SgnsError):
+            t.upload(np.array([1, -2, 3, -1], np.int32))
+
+
+def test_empty_and_degenerate_corpora(sgns_lib):
+    opt = sgns.default_options(size=8, window=2, negative=2, iter=2, debug=0, table_size=1000)
+    for eng in ("plain", "persistent"):
+        opt.engine = {"plain": 0, "persistent": 1}[eng]
+        with sgns.Trainer(opt) as t:
+            t.set_vocab(np.ones(10, np.int32))
+            w0 = t.embeddings(0)
+            st = t.train_corpus(np.array([], np.int32))
+            assert st.steps == 0
+            st = t.train_corpus(np.array([-1, -1, 3, -1, 4, -1], np.int32))  # only length-1 walks
+            assert st.steps == 0
+            assert np.array_equal(t.embeddings(0), w0)

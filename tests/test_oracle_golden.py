@@ -1,0 +1,67 @@
+"""The oracle against the reference's own outputs (tests/golden/, made by
+tests/golden/make_golden.py from the unmodified include/dsgl.hpp)."""
+import glob
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CASES = sorted(os.path.basename(p)[:-5] for p in glob.glob(os.path.join(GOLDEN, "*.json")))
+
+
+def load(name):
+    meta = json.load(open(os.path.join(GOLDEN, name + ".json")))
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    return meta, z["corpus"], z["order"]
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def test_cases_present():
+    assert len(CASES) >= 5
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_matches_reference_bit_for_bit(name, oracle_mod):
+    meta, corpus, order = load(name)
+    counts = np.bincount(corpus[corpus >= 0], minlength=meta["V"]).astype(np.int32)
+    wih, woh, st = oracle_mod.train(corpus, counts, d=meta["d"], window=meta["window"],
+                                    negative=meta["negative"], iter=meta["iter"], workers=1, threads=1,
+                                    table_threads=meta["table_threads"], policy=oracle_mod.POLICY_REF,
+                                    storage=oracle_mod.STORE_F32, table_size=meta["table_size"],
+                                    sample=meta["sample"], alpha=meta["alpha"])
+    o, _, _, _ = oracle_mod.vocab(counts)
+    assert np.array_equal(o, order)
+    assert sha(wih) == meta["wih_sha256"], np.abs(wih[0] - np.array(meta["wih_row0"], np.float32)).max()
+    assert sha(woh) == meta["woh_sha256"]
+    assert st["steps"] > 0
+
+
+def test_sigmoid_table_matches_reference(oracle_mod):
+    meta, _, _ = load(CASES[0])
+    assert sha(oracle_mod.exp_table()) == meta["exp_sha256"]
+
+
+@pytest.mark.parametrize("name", CASES[:2])
+def test_unigram_table_matches_reference(name, oracle_mod):
+    meta, corpus, _ = load(name)
+    counts = np.bincount(corpus[corpus >= 0], minlength=meta["V"]).astype(np.int32)
+    _, _, cns, _ = oracle_mod.vocab(counts)
+    t = oracle_mod.unigram_table(cns, meta["table_size"], meta["table_threads"])
+    assert sha(t) == meta["table_sha256"]
+
+
+def test_init_matches_reference_lcg(oracle_mod):
+    # dsgl.hpp:451-456 restated independently in Python
+    V, d = 3, 4
+    w = oracle_mod.init_wih(V, d).reshape(-1)
+    r = 1
+    for i in range(V * d):
+        r = (r * 25214903917 + 11) % (1 << 64)
+        v = np.float32((np.float32(r & 0xFFFF) / np.float32(65536.0)) - np.float32(0.5)) / np.float32(d)
+        assert w[i] == np.float32(v)
