@@ -123,9 +123,10 @@ template <int DT>
 __global__ void __launch_bounds__(32) adjoint_kernel(int d, int n, const int32_t* in_ptr, const int32_t* in_ids,
                                                      const int32_t* in_first, const int32_t* out_ptr,
                                                      const int32_t* out_ids, const int32_t* out_meta,
-                                                     const void* wih, const void* woh, const int32_t* incl_in,
-                                                     const int32_t* incl_out, typename Elem<DT>::T* g_in,
-                                                     typename Elem<DT>::T* g_out, double* loss_out) {
+                                                     const void* wih, const void* woh, int64_t V,
+                                                     const int32_t* incl_in, const int32_t* incl_out,
+                                                     typename Elem<DT>::T* g_in, typename Elem<DT>::T* g_out,
+                                                     double* loss_out) {
   typedef typename Elem<DT>::T T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
@@ -133,6 +134,11 @@ __global__ void __launch_bounds__(32) adjoint_kernel(int d, int n, const int32_t
   if (b >= n) return;
   const int i0 = in_ptr[b], I = in_ptr[b + 1] - i0, o0 = out_ptr[b], O = out_ptr[b + 1] - o0;
   const int first = in_first[b];
+  // ids outside [0, V) were flagged by mark_rows_kernel; this minibatch is skipped
+  bool ok = true;
+  for (int j = lane; j < I; j += 32) ok &= in_ids[i0 + j] >= 0 && in_ids[i0 + j] < V;
+  for (int i = lane; i < O; i += 32) ok &= out_ids[o0 + i] >= 0 && out_ids[o0 + i] < V;
+  if (!__all_sync(kFull, ok)) return;
   T* x = sm;                           // I x d
   T* o = x + (size_t)I * d;            // O x d
   T* coef = o + (size_t)O * d;         // O x I
@@ -227,19 +233,19 @@ cudaError_t launch_adjoint(int dtype, int d, int n, int64_t V, int64_t total_in,
       if ((e = cudaFuncSetAttribute(adjoint_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
         return e;
       adjoint_kernel<2><<<n, 32, smem, s>>>(d, n, in_ptr, in_ids, in_first, out_ptr, out_ids, out_meta, wih, woh,
-                                            incl_in, incl_out, static_cast<double*>(grad_in),
+                                            V, incl_in, incl_out, static_cast<double*>(grad_in),
                                             static_cast<double*>(grad_out), loss);
     } else if (dtype == 1) {
       if ((e = cudaFuncSetAttribute(adjoint_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
         return e;
       adjoint_kernel<1><<<n, 32, smem, s>>>(d, n, in_ptr, in_ids, in_first, out_ptr, out_ids, out_meta, wih, woh,
-                                            incl_in, incl_out, static_cast<float*>(grad_in),
+                                            V, incl_in, incl_out, static_cast<float*>(grad_in),
                                             static_cast<float*>(grad_out), loss);
     } else {
       if ((e = cudaFuncSetAttribute(adjoint_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
         return e;
       adjoint_kernel<0><<<n, 32, smem, s>>>(d, n, in_ptr, in_ids, in_first, out_ptr, out_ids, out_meta, wih, woh,
-                                            incl_in, incl_out, static_cast<float*>(grad_in),
+                                            V, incl_in, incl_out, static_cast<float*>(grad_in),
                                             static_cast<float*>(grad_out), loss);
     }
   }

@@ -138,6 +138,10 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
       const unsigned fr = __ballot_sync(kFull, lane < NS && wref[lane] == 0);
       s = __ffs(fr) - 1;
       fresh = true;
+      if (s < 0) {  // cannot happen: at most 2w+2 distinct vertices are resident
+        if (lane == 0) atomicExch(&p.ctr->status, 2);
+        s = 0;
+      }
     }
     __syncwarp();
     if (lane == 0) {

@@ -205,7 +205,8 @@ sgns_status finish_stats(sgns_handle* h, int workers, float ms) {
   CU(h, cudaMemcpyAsync(h->h_ctr, h->d_ctr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost, h->stream));
   CU(h, cudaStreamSynchronize(h->stream));
   const DeviceCounters& c = *h->h_ctr;
-  if (c.status != 0) return fail(h, SGNS_EINVAL, "kernel reported a walk longer than the staged capacity");
+  if (c.status == 1) return fail(h, SGNS_EINVAL, "kernel reported a walk longer than the staged capacity");
+  if (c.status != 0) return fail(h, SGNS_EINVAL, "kernel reported an internal inconsistency (code %d)", c.status);
   sgns_stats& s = h->stats;
   s.steps = c.steps;
   s.pairs = c.pairs;
