@@ -1,0 +1,359 @@
+"""Benchmark of the DSGL skip-gram negative-sampling trainer on one GB300 (or N replicas).
+
+Workload (default "lj-cl"): a seeded Chung-Lu power-law graph with LiveJournal's vertex
+count (2,238,731 vertices, ~30M edges, exponent 2.1), 10% of its edges held out for link
+prediction; corpus = 10 uniform random walks per vertex on the remaining graph, lengths
+geometric with mean 40 capped at 80 (~0.8e9 tokens); d=128, window 10, 5 negatives,
+sample 1e-3, alpha 0.01, unigram table 1e8.  One step = one training pass over the whole
+corpus (sgns_train: the persistent kernel, replayed from its CUDA graph) with bf16 tables
+and stochastic rounding.  The tables (1.1 GB) and the corpus (3.2 GB) are far larger than
+the 129 MB L2, so no flush is needed between steps.
+
+Printed JSON line: value = pairs/s over the timed steps (all ranks), e2e = the same metric
+through sgns_train_corpus from pinned host memory (upload + mapping + training + stats
+read-back per step), roofline of the persistent kernel (row-traffic bytes of the reference
+step, 2*(I+O)*d*2 B per minibatch, over its CUDA-event time), the plain fp32 engine on a
+1/8 slice of the same corpus, the CPU baseline (the oracle restatement of the reference
+trainer on the host cores, bounded sample), link-prediction AUC of the trained embedding.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload lj-cl|small]
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "gdistger-re_gb300"), os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "SGNS pairs/sec on 1 GB300 (BF16 batched vs plain FP32, same AUC) + HBM roofline %"
+
+WORKLOADS = {
+    "lj-cl": dict(V=2238731, E=30_000_000, gamma=2.1, walks=10, mean=40, cap=80),
+    "small": dict(V=200_000, E=2_000_000, gamma=2.1, walks=10, mean=40, cap=80),
+}
+TRAIN = dict(size=128, window=10, negative=5, sample=1e-3, alpha=0.01, table_size=100_000_000, threads=12)
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names[1:], parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_corpus(wl, rank, device):
+    import torch
+    import synth
+
+    t0 = time.time()
+    ip, ix = synth.chung_lu(wl["V"], wl["E"], wl["gamma"], seed=2024, device=device)
+    tr_ip, tr_ix, pos, neg = synth.holdout(ip, ix, 0.1, seed=7)
+    n_walks = wl["V"] * wl["walks"]
+    L = synth.walk_lengths(n_walks, "geometric", mean=wl["mean"], cap=wl["cap"], seed=100 + rank, device=device)
+    corpus = synth.random_walks(tr_ip, tr_ix, wl["walks"], L, seed=200 + rank)
+    edges = int(ix.numel() // 2)
+    del ip, ix, tr_ix
+    torch.cuda.synchronize()
+    return corpus, pos, neg, edges, time.time() - t0
+
+
+def cpu_baseline(corpus_host, V, seconds_hint=12.0, tokens=None):
+    """The oracle restatement of the reference trainer (reference buffer policy, fp32),
+    Hogwild over every host core, on the first `tokens` tokens of the corpus."""
+    import oracle
+
+    cores = os.cpu_count() or 1
+    if tokens is None:
+        tokens = int(max(200_000, min(len(corpus_host), cores * 70_000 * seconds_hint / 12.0)))
+    sample = np.ascontiguousarray(corpus_host[:tokens])
+    counts = np.bincount(corpus_host[corpus_host >= 0], minlength=V).astype(np.int32)
+    t0 = time.time()
+    _, _, st = oracle.train(sample, counts, d=TRAIN["size"], window=TRAIN["window"], negative=TRAIN["negative"],
+                            iter=1, workers=cores, threads=cores, table_threads=TRAIN["threads"],
+                            policy=oracle.POLICY_REF, storage=oracle.STORE_F32, table_size=TRAIN["table_size"],
+                            sample=TRAIN["sample"], alpha=TRAIN["alpha"])
+    wall = time.time() - t0
+    return st, wall, cores, tokens
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0, None
+    import torch.distributed as dist
+
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    dist.init_process_group("nccl" if os.environ.get("BENCH_BACKEND", "nccl") == "nccl" else "gloo")
+    return rank, ws, local, dist
+
+
+def max_over_ranks(x, dist, device):
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x, dist, device):
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def run_reference(args, wl):
+    """Reference arm: the reference's CPU trainer restated (oracle), every host thread."""
+    rank, ws, local, dist = dist_setup()
+    if rank != 0:
+        return
+    import torch
+    import synth
+
+    ip, ix = synth.chung_lu(wl["V"], wl["E"], wl["gamma"], seed=2024, device="cpu")
+    tr_ip, tr_ix, _, _ = synth.holdout(ip, ix, 0.1, seed=7)
+    cores = os.cpu_count() or 1
+    # walks of a vertex subset are enough for a bounded sample per step
+    nw = min(wl["V"] * wl["walks"], max(20000, cores * 2500))
+    starts_graph = (tr_ip, tr_ix)
+    L = synth.walk_lengths(wl["V"] * 1, "geometric", mean=wl["mean"], cap=wl["cap"], seed=100)
+    corpus = synth.random_walks(tr_ip, tr_ix, 1, L, seed=200).numpy().astype(np.int32)
+    ends = np.flatnonzero(corpus == -1)
+    cut = ends[min(len(ends) - 1, nw)] + 1
+    corpus_s = corpus[:cut]
+    counts_full = synth.vertex_counts(corpus, wl["V"]).numpy()
+    import oracle
+
+    times, pairs = [], []
+    for it in range(args.warmup + args.steps):
+        t0 = time.time()
+        _, _, st = oracle.train(corpus_s, counts_full, d=TRAIN["size"], window=TRAIN["window"],
+                                negative=TRAIN["negative"], iter=1, workers=cores, threads=cores,
+                                table_threads=TRAIN["threads"], policy=oracle.POLICY_REF,
+                                storage=oracle.STORE_F32, table_size=TRAIN["table_size"],
+                                sample=TRAIN["sample"], alpha=TRAIN["alpha"])
+        dt = time.time() - t0
+        if it >= args.warmup:
+            times.append(dt)
+            pairs.append(st["pairs"])
+    value = sum(pairs) / sum(times)
+    sample = ("%d walks (%d tokens) of the %s corpus per step, d=128 w=10 K=5 fp32, reference buffer policy, "
+              "table 1e8; oracle restatement of include/dsgl.hpp (the reference's own build cannot run on "
+              "this host: its sources are not shipped to it)" % (min(nw, len(ends)), cut, args.workload))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "data": "synthetic", "config": {"workload": args.workload + " (CPU sample)", **TRAIN},
+            "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="lj-cl", choices=sorted(WORKLOADS))
+    ap.add_argument("--skip-extras", action="store_true", help="only the timed bf16 steps (profiling runs)")
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, wl)
+
+    import torch
+
+    rank, ws, local, dist = dist_setup()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    import sgns
+
+    if not os.path.exists(sgns.LIB_PATH):
+        import build as sgns_build
+
+        sgns_build.build()
+
+    corpus, pos, neg, edges, gen_s = make_corpus(wl, rank, dev)
+    n_tok = int(corpus.numel())
+    counts = torch.bincount(corpus[corpus >= 0].long(), minlength=wl["V"]).to(torch.int32).cpu().numpy()
+    corpus_host = torch.empty(n_tok, dtype=torch.int32, pin_memory=True)
+    corpus_host.copy_(corpus.cpu())
+    host_np = corpus_host.numpy()
+
+    opt = sgns.default_options(iter=1, storage="bf16", engine="persistent", device=local, debug=0, **TRAIN)
+    tr = sgns.Trainer(opt)
+    tr.set_vocab(counts)
+    tr.upload(host_np)
+    for _ in range(args.warmup):
+        tr.train()
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    kernel_ms, pairs, row_bytes, st = [], 0, 0, None
+    for _ in range(args.steps):
+        st = tr.train()
+        kernel_ms.append(st.train_ms)
+        pairs += st.pairs
+        row_bytes += st.row_bytes
+    torch.cuda.synchronize()
+    elapsed = time.perf_counter() - t0
+    if dist is not None:
+        dist.barrier()
+    clk = clocks.stop()
+    elapsed_max = max_over_ranks(elapsed, dist, dev)
+    total_pairs = sum_over_ranks(float(pairs), dist, dev)
+    value = total_pairs / elapsed_max
+    st_last = st
+
+    # roofline of the persistent kernel: row-traffic bytes per launch / CUDA-event time
+    pk = peaks()
+    launch_s = float(np.mean(kernel_ms)) / 1e3
+    bytes_per_launch = row_bytes / args.steps
+    achieved = bytes_per_launch / launch_s / 1e9
+    peak = pk["hbm_gbs"] if pk else 6800.0
+    table_traffic = (st_last.row_loads + st_last.row_stores + 2 * st_last.output_rows) * TRAIN["size"] * 2
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "peak_source": "measured" if pk else "fallback",
+                "algorithmic_bytes_per_launch": bytes_per_launch,
+                "table_bytes_per_launch": float(table_traffic + 4 * n_tok),
+                "kernel_ms": float(np.mean(kernel_ms))}
+    line = {"metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * elapsed_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
+            "data": "synthetic (seeded Chung-Lu stand-in for LiveJournal; random walks)",
+            "config": {"workload": "%s: Chung-Lu V=%d E=%d gamma=%.1f, 10 walks/vertex geometric(mean %d, cap %d) "
+                                   "on the 90%% training graph, %d tokens per rank" %
+                                   (args.workload, wl["V"], edges, wl["gamma"], wl["mean"], wl["cap"], n_tok),
+                       "engine": "persistent", "storage": "bf16-sr", "workers": st_last.workers,
+                       "warps_per_cta": st_last.warps_per_cta, "l2": "inputs larger than L2 (no flush)",
+                       "parallelism": "replicas x%d" % ws, **TRAIN},
+            "roofline": roofline, "gpu_launches": args.steps, "clocks": clk,
+            "steps_per_launch": st_last.steps, "pairs_per_launch": st_last.pairs, "corpus_gen_s": gen_s}
+
+    if not args.skip_extras:
+        # e2e through the reference-facing call, host buffers in, statistics out
+        e2e_t, e2e_pairs = [], 0
+        for it in range(max(1, args.steps)):
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            s2 = tr.train_corpus_ptr(corpus_host.data_ptr(), n_tok)
+            t2 = time.perf_counter()
+            e2e_t.append(t2 - t1)
+            e2e_pairs += s2.pairs
+        e2e_max = max_over_ranks(sum(e2e_t), dist, dev)
+        e2e_pairs_all = sum_over_ranks(float(e2e_pairs), dist, dev)
+        line["e2e"] = {"value": e2e_pairs_all / e2e_max, "unit": "pairs/s", "h2d_bytes_per_step": 4 * n_tok,
+                       "d2h_bytes_per_step": 80}
+        line["gpu_launches"] = args.steps + 3 * max(1, args.steps)
+        # link prediction on the held-out edges (rows mapped back to vertex ids)
+        import synth
+
+        order = tr.order()
+        emb = np.zeros((wl["V"], TRAIN["size"]), np.float32)
+        emb[order] = tr.embeddings(0)
+        line["auc_bf16"] = synth.link_auc(emb, pos, neg)
+        tr.close()
+        # plain fp32 engine (reference buffer policy, one launch per step) on a 1/8 slice
+        ends = torch.nonzero(corpus == -1).flatten()
+        cut = int(ends[len(ends) // 8]) + 1
+        popt = sgns.default_options(iter=1, storage="fp32", engine="plain", device=local, debug=0, **TRAIN)
+        with sgns.Trainer(popt) as pt:
+            pt.set_vocab(counts)
+            pt.upload(host_np[:cut])
+            pt.train()
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            ps = pt.train()
+            t2 = time.perf_counter()
+        line["plain_fp32"] = {"value": ps.pairs / (t2 - t1), "unit": "pairs/s", "tokens": cut,
+                              "workers": ps.workers, "kernel_ms": ps.train_ms}
+        line["bf16_persistent_over_plain_fp32"] = value / ws / line["plain_fp32"]["value"]
+        if rank == 0:
+            cst, wall, cores, toks = cpu_baseline(host_np, wl["V"])
+            line["cpu_baseline"] = {"value": cst["pairs"] / wall, "unit": "pairs/s", "cores": cores, "kind": "port",
+                                    "sample": "first %d tokens of the corpus, d=128 w=10 K=5 fp32, reference buffer "
+                                              "policy, %d Hogwild threads (oracle restatement of include/dsgl.hpp)"
+                                              % (toks, cores)}
+    else:
+        tr.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

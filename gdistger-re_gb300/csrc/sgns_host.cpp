@@ -217,6 +217,9 @@ sgns_status finish_stats(sgns_handle* h, int workers, float ms) {
   s.train_ms = ms;
   s.workers = workers;
   s.warps_per_cta = h->opt.engine == SGNS_ENGINE_PERSISTENT ? h->wpc : 4;
+  s.row_loads = c.row_loads;
+  s.row_stores = c.row_stores;
+  s.output_rows = c.outputs;
   return SGNS_OK;
 }
 

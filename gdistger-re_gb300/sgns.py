@@ -36,6 +36,7 @@ class Stats(ctypes.Structure):
         ("steps", ctypes.c_uint64), ("pairs", ctypes.c_uint64), ("word_count_actual", ctypes.c_uint64),
         ("row_bytes", ctypes.c_uint64), ("loss", ctypes.c_double), ("final_alpha", ctypes.c_float),
         ("train_ms", ctypes.c_float), ("workers", ctypes.c_int32), ("warps_per_cta", ctypes.c_int32),
+        ("row_loads", ctypes.c_uint64), ("row_stores", ctypes.c_uint64), ("output_rows", ctypes.c_uint64),
     ]
 
     def as_dict(self):

@@ -100,24 +100,26 @@ def holdout(indptr, indices, frac=0.1, seed=7):
     m = src.numel()
     want = int(m * frac)
     perm = torch.randperm(m, generator=g, device=dev)
-    deg = (indptr[1:] - indptr[:-1]).clone()
+    deg = indptr[1:] - indptr[:-1]
     cand = perm[: min(m, int(want * 1.5) + 16)]
     cs, cd = src[cand], dst[cand]
-    # greedy removal in candidate order while degrees stay > 1 (vectorised in rounds)
-    removed = torch.zeros(cand.numel(), dtype=torch.bool, device=dev)
-    cs_l, cd_l, deg_l = cs.cpu().numpy(), cd.cpu().numpy(), deg.cpu().numpy()
-    rem_l = np.zeros(cand.numel(), dtype=bool)
-    taken = 0
-    for k in range(cand.numel()):
-        if taken >= want:
-            break
-        a, b = cs_l[k], cd_l[k]
-        if deg_l[a] > 2 and deg_l[b] > 2:
-            deg_l[a] -= 1
-            deg_l[b] -= 1
-            rem_l[k] = True
-            taken += 1
-    removed = torch.from_numpy(rem_l).to(dev)
+    # a candidate is removed when, counting every earlier candidate at each endpoint as
+    # removed too, both endpoints keep degree > 1 (a conservative, vectorised form of the
+    # sequential rule)
+    ends = torch.cat([cs, cd])
+    pos_in = torch.arange(ends.numel(), device=dev)
+    order = torch.argsort(ends * ends.numel() + pos_in % cand.numel())
+    sorted_ends = ends[order]
+    first_of_run = torch.ones_like(sorted_ends, dtype=torch.bool)
+    first_of_run[1:] = sorted_ends[1:] != sorted_ends[:-1]
+    run_start = torch.cummax(torch.where(first_of_run, torch.arange(ends.numel(), device=dev),
+                                         torch.zeros_like(pos_in)), 0).values
+    rank_sorted = torch.arange(ends.numel(), device=dev) - run_start
+    rank = torch.empty_like(rank_sorted)
+    rank[order] = rank_sorted
+    ra, rb = rank[: cand.numel()], rank[cand.numel():]
+    ok = (deg[cs] - ra > 2) & (deg[cd] - rb > 2)
+    removed = ok & (torch.cumsum(ok.long(), 0) <= want)
     test_ids = cand[removed]
     keep = torch.ones(m, dtype=torch.bool, device=dev)
     keep[test_ids] = False

@@ -82,6 +82,9 @@ typedef struct sgns_stats {
   float train_ms;              /* device time of the last training call              */
   int32_t workers;
   int32_t warps_per_cta;
+  uint64_t row_loads;          /* table rows copied into worker buffers              */
+  uint64_t row_stores;         /* table rows written back from worker buffers        */
+  uint64_t output_rows;        /* sum over steps of the output rows (targets + negatives) */
 } sgns_stats;
 
 /* Defaults of dsgl.hpp:67-76, table_size 1e8, persistent engine, fp32. */
