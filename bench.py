@@ -224,6 +224,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="lj-cl", choices=sorted(WORKLOADS))
     ap.add_argument("--skip-extras", action="store_true", help="only the timed bf16 steps (profiling runs)")
+    ap.add_argument("--wpc", type=int, default=0, help="warps per CTA of the persistent engine (0 = autotune)")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
@@ -248,7 +249,8 @@ def main():
     corpus_host.copy_(corpus.cpu())
     host_np = corpus_host.numpy()
 
-    opt = sgns.default_options(iter=1, storage="bf16", engine="persistent", device=local, debug=0, **TRAIN)
+    opt = sgns.default_options(iter=1, storage="bf16", engine="persistent", device=local, debug=0,
+                               warps_per_cta=args.wpc, **TRAIN)
     tr = sgns.Trainer(opt)
     tr.set_vocab(counts)
     tr.upload(host_np)

@@ -27,7 +27,7 @@ constexpr int kHdrWords = 1004 + 132;  // sigmoid table (1001 -> 1004) + SmallJu
 
 struct WinLayout {  // per-warp shared memory, in 4-byte words
   int NS, R, DP, OP, OM, IM, lmax;
-  int rows, corr, sen, vert, ref, ring, inrow, outid, outmeta, words;
+  int rows, corr, sen, vert, ref, ring, inrow, outid, outmeta, pend, words;
 };
 
 __host__ __device__ inline WinLayout win_layout(int d, int w, int K, int lmax) {
@@ -58,6 +58,8 @@ __host__ __device__ inline WinLayout win_layout(int d, int w, int K, int lmax) {
   off += L.OM;
   L.outmeta = off;
   off += L.OM;
+  L.pend = off;  // pending row loads: ids, then destination rows
+  off += 2 * (w + 1);
   L.words = (off + 3) & ~3;
   return L;
 }
@@ -68,6 +70,38 @@ __device__ __forceinline__ void load_row_to_smem(const void* tab, int64_t row, i
   for (int q = lane_id(); q < d4; q += 32)
     reinterpret_cast<float4*>(dst)[q] = RowIO<S>::load4(tab, row, d, q);
 }
+// Loads up to NB rows (ids[0..n)) into registers before storing any of them, so their
+// DRAM round trips overlap; dst(u) is the shared-memory row of the u-th id.
+template <int S, int DCH, int NB, class Dst>
+__device__ __forceinline__ void load_rows_batched(const void* tab, const int* ids, int n, int d, Dst dst) {
+  const int lane = lane_id(), d4 = d >> 2;
+  for (int b0 = 0; b0 < n; b0 += NB) {
+    float4 v[NB][DCH];
+#pragma unroll
+    for (int u = 0; u < NB; u++) {
+      if (b0 + u < n) {
+        const int row = ids[b0 + u];
+#pragma unroll
+        for (int t = 0; t < DCH; t++) {
+          const int q = lane + 32 * t;
+          if (q < d4) v[u][t] = RowIO<S>::load4(tab, row, d, q);
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < NB; u++) {
+      if (b0 + u < n) {
+        float4* out = reinterpret_cast<float4*>(dst(b0 + u));
+#pragma unroll
+        for (int t = 0; t < DCH; t++) {
+          const int q = lane + 32 * t;
+          if (q < d4) out[q] = v[u][t];
+        }
+      }
+    }
+  }
+}
+
 template <int S>
 __device__ __forceinline__ void store_row_from_smem(void* tab, int64_t row, int d, const float* src,
                                                     uint64_t ev) {
@@ -105,6 +139,8 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
   int* in_row = reinterpret_cast<int*>(base + L.inrow);
   int* out_id = reinterpret_cast<int*>(base + L.outid);
   int* out_meta = reinterpret_cast<int*>(base + L.outmeta);
+  int* pend_id = reinterpret_cast<int*>(base + L.pend);
+  int* pend_row = pend_id + (w + 1);
   const int NS = L.NS, R = L.R, DP = L.DP, lmax = L.lmax;
 
   // dsgl.hpp:790-826
@@ -125,7 +161,9 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
   unsigned long long n_pairs = 0, n_steps = 0, n_outs = 0, n_loads = 0, n_stores = 0;
   __syncwarp();
 
-  auto enter = [&](int walk, int position) -> bool {  // true if a row must be loaded
+  // Places position `position` of walk `walk` in the window: an existing slot of the same
+  // vertex, or a free slot.  Returns the slot; *fresh says the row must be loaded.
+  auto enter_assign = [&](int walk, int position, bool* fresh_out) -> int {
     const int v = sen[walk * lmax + position];
     int* wref = ref + walk * NS;
     int* wvert = vert + walk * NS;
@@ -150,11 +188,27 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
       ring[walk * R + position % R] = s;
     }
     __syncwarp();
-    if (fresh) {
-      load_row_to_smem<S>(p.wih, v, d, rows + (size_t)(walk * NS + s) * DP);
-      n_loads++;
+    *fresh_out = fresh;
+    return s;
+  };
+  // the first window of a freshly loaded walk: slots first, then one batched load
+  auto enter_initial = [&](int walk, int hi) {
+    int n = 0;
+    for (int q = 0; q <= hi; q++) {
+      bool fresh;
+      const int s = enter_assign(walk, q, &fresh);
+      if (fresh) {
+        if (lane == 0) {
+          pend_id[n] = vert[walk * NS + s];
+          pend_row[n] = walk * NS + s;
+        }
+        n++;
+      }
     }
-    return fresh;
+    __syncwarp();
+    load_rows_batched<S, DCH, (DCH == 1 ? 8 : 4)>(p.wih, pend_id, n, d, [&](int u) { return rows + (size_t)pend_row[u] * DP; });
+    n_loads += (unsigned long long)n;
+    __syncwarp();
   };
   auto leave = [&](int walk, int position, uint64_t ev) {
     const int s = ring[walk * R + position % R];
@@ -198,8 +252,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
         if (n <= 1) continue;
         len[walk] = n;
         pos[walk] = 0;
-        const int hi = n - 1 < w ? n - 1 : w;
-        for (int q = 0; q <= hi; q++) enter(walk, q);
+        enter_initial(walk, n - 1 < w ? n - 1 : w);
       }
     }
     if (cur >= end) {  // dsgl.hpp:1031-1050
@@ -238,14 +291,8 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     grp_g = g;
     grp_state = gs;
     const int O = select_outputs(p, *sj, gs, t1, t2, out_id, out_meta);
-    {  // gather the output rows (targets and negatives) from Woh
-      const int d4 = d >> 2;
-      for (int i = 0; i < O; i++) {
-        const int row = out_id[i];
-        for (int q = lane; q < d4; q += 32)
-          reinterpret_cast<float4*>(out_rows + (size_t)i * DP)[q] = RowIO<S>::load4(p.woh, row, d, q);
-      }
-    }
+    // gather the output rows (targets and negatives) from Woh, all loads in flight at once
+    load_rows_batched<S, DCH, (DCH == 1 ? kOMax : 4)>(p.woh, out_id, O, d, [&](int u) { return out_rows + (size_t)u * DP; });
     __syncwarp();
     const float alpha = *reinterpret_cast<volatile float*>(&p.ctr->alpha);
     auto in_ptr = [&](int j) -> const float* { return rows + (size_t)in_row[j] * DP; };
@@ -294,18 +341,51 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     // ---- positions, window moves, walk ends (dsgl.hpp:1372-1407) ----
     pos[0]++;
     pos[1]++;
-    for (int walk = 0; walk < 2; walk++) {
-      const uint64_t ev =
-          S == STORE_BF16 ? sr_event_key(p.sr_seed, EV_WALK0 + walk, (uint32_t)wid, step_id) : 0;
-      if (pos[walk] >= len[walk]) {
-        flush_walk(walk, ev);
-        len[walk] = 0;
-        train_sen_num++;
-      } else {
-        const int P = pos[walk];
-        if (P + w < len[walk]) enter(walk, P + w);
-        if (P - w - 1 >= 0) leave(walk, P - w - 1, ev);
+    {
+      // The memory order of the oracle: walk 0 (enter, leave), then walk 1 (enter, leave).
+      // An entering row's load is issued into registers at its place in that order and
+      // written to its slot after all four operations, so the loads overlap.
+      float4 ent[2][DCH];
+      int ent_row[2] = {-1, -1};
+      const int d4 = d >> 2;
+      for (int walk = 0; walk < 2; walk++) {
+        const uint64_t ev =
+            S == STORE_BF16 ? sr_event_key(p.sr_seed, EV_WALK0 + walk, (uint32_t)wid, step_id) : 0;
+        if (pos[walk] >= len[walk]) {
+          flush_walk(walk, ev);
+          len[walk] = 0;
+          train_sen_num++;
+        } else {
+          const int P = pos[walk];
+          if (P + w < len[walk]) {
+            bool fresh;
+            const int s = enter_assign(walk, P + w, &fresh);
+            if (fresh) {
+              const int v = vert[walk * NS + s];
+#pragma unroll
+              for (int t = 0; t < DCH; t++) {
+                const int q = lane + 32 * t;
+                if (q < d4) ent[walk][t] = RowIO<S>::load4(p.wih, v, d, q);
+              }
+              ent_row[walk] = walk * NS + s;
+              n_loads++;
+            }
+          }
+          if (P - w - 1 >= 0) leave(walk, P - w - 1, ev);
+        }
       }
+#pragma unroll
+      for (int walk = 0; walk < 2; walk++) {
+        if (ent_row[walk] >= 0) {
+          float4* dst = reinterpret_cast<float4*>(rows + (size_t)ent_row[walk] * DP);
+#pragma unroll
+          for (int t = 0; t < DCH; t++) {
+            const int q = lane + 32 * t;
+            if (q < d4) dst[q] = ent[walk][t];
+          }
+        }
+      }
+      __syncwarp();
     }
     if (train_sen_num >= 2) {
       change_neg = true;
