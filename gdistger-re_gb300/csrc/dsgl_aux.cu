@@ -59,12 +59,13 @@ __global__ void __launch_bounds__(32) minibatch_kernel(int d, int imax, int omax
     if (lane == 0) atomicExch(status, 1);
     return;
   }
-  const int DP = d + 4, OP = (omax + 3) & ~3;
+  const int DP = d + 4;
   float* exp_s = smem;
   float* xin = smem + 1004;
   float* xout = xin + (size_t)imax * DP;
-  float* corrT = xout + (size_t)omax * DP;
-  int* meta = reinterpret_cast<int*>(corrT + (size_t)imax * OP);
+  float* outI = xout + (size_t)kOMax * DP;
+  float2* corrP = reinterpret_cast<float2*>(outI + (size_t)kOMax * d);
+  int* meta = reinterpret_cast<int*>(corrP + (size_t)imax * (kOMax + 2));
   for (int i = lane; i < kExpTableSize + 1; i += 32) exp_s[i] = exp_table[i];
   const int d4 = d >> 2;
   const float* gin = in_rows + in_off[b] * d;
@@ -72,18 +73,27 @@ __global__ void __launch_bounds__(32) minibatch_kernel(int d, int imax, int omax
   for (int j = 0; j < I; j++)
     for (int q = lane; q < d4; q += 32)
       reinterpret_cast<float4*>(xin + (size_t)j * DP)[q] = reinterpret_cast<const float4*>(gin + (size_t)j * d)[q];
-  for (int i = 0; i < O; i++)
-    for (int q = lane; q < d4; q += 32)
-      reinterpret_cast<float4*>(xout + (size_t)i * DP)[q] = reinterpret_cast<const float4*>(gout + (size_t)i * d)[q];
+  {
+    float4 v[kOMax][DCH];
+#pragma unroll
+    for (int i = 0; i < kOMax; i++)
+#pragma unroll
+      for (int t = 0; t < DCH; t++) {
+        const int q = lane + 32 * t;
+        v[i][t] = (i < O && q < d4) ? reinterpret_cast<const float4*>(gout + (size_t)i * d)[q]
+                                    : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    store_out_rows<kOMax, DCH>(v, O, d, xout, DP, outI);
+  }
   for (int i = lane; i < O; i += 32) meta[i] = out_meta_all[out_off[b] + i];
   __syncwarp();
   auto in_ptr = [&](int j) -> const float* { return xin + (size_t)j * DP; };
   float loss = 0.f;
-  forward_gradient(I, first, O, d, in_ptr, xout, DP, meta, exp_s, alpha[b], corrT, OP, false, loss);
+  forward_gradient<kOMax>(I, first, O, d, in_ptr, outI, meta, exp_s, alpha[b], corrP, false, loss);
   float4 md[kOMax][DCH];
   float* gdin = d_in + in_off[b] * d;
-  backward<DCH>(I, O, d, in_ptr, xout, DP, corrT, OP, md,
-                [&](int j, int q, float4 a) { reinterpret_cast<float4*>(gdin + (size_t)j * d)[q] = a; });
+  backward<kOMax, DCH>(I, O, d, in_ptr, xout, DP, corrP, md,
+                       [&](int j, int q, float4 a) { reinterpret_cast<float4*>(gdin + (size_t)j * d)[q] = a; });
   float* gdout = d_out + out_off[b] * d;
 #pragma unroll
   for (int i = 0; i < kOMax; i++)
@@ -154,8 +164,10 @@ cudaError_t launch_minibatch(int d, int n, int imax, int omax, const int32_t* in
   int64_t* in_off = offsets;
   int64_t* out_off = offsets + n;
   prefix_offsets_kernel<<<1, 1, 0, s>>>(in_count, out_count, n, in_off, out_off);
-  const int DP = d + 4, OP = (omax + 3) & ~3;
-  const size_t smem = sizeof(float) * (1004 + (size_t)(imax + omax) * DP + (size_t)imax * OP + omax + 4);
+  const int DP = d + 4;
+  (void)omax;
+  const size_t smem = sizeof(float) * (1004 + (size_t)(imax + kOMax) * DP + (size_t)kOMax * d +
+                                       (size_t)imax * (kOMax + 2) * 2 + kOMax + 4);
   cudaError_t e;
   if (d > 128) {
     e = cudaFuncSetAttribute(minibatch_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

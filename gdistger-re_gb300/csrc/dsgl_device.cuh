@@ -225,20 +225,6 @@ __device__ __forceinline__ int select_outputs_stored(int K, const int* words, in
   return O;
 }
 
-// trainers: buffered input row += update
-template <class InPtr>
-struct AddToInput {
-  InPtr in_ptr;
-  __device__ __forceinline__ void operator()(int j, int q, float4 a) const {
-    float4* x = reinterpret_cast<float4*>(const_cast<float*>(in_ptr(j)));
-    x[q] = add4(x[q], a);
-  }
-};
-template <class InPtr>
-__device__ __forceinline__ AddToInput<InPtr> add_to_input(InPtr f) {
-  return AddToInput<InPtr>{f};
-}
-
 // ---- window input list (dsgl.hpp:1100-1132) ------------------------------------------
 // Appends the positions c = pos - w + i, i in [b, 2w+1-b), i != w, 0 <= c < len in
 // increasing order; slot_of(c) gives the row index stored in in_row.  Returns the count.
@@ -259,44 +245,62 @@ __device__ __forceinline__ int window_inputs(int pos, int len, int w, int b, int
 }
 
 // ---- step arithmetic ---------------------------------------------------------------
-// in_ptr(j) -> const float* row of input j (16-byte aligned; shared or global memory).
-// out_rows: O float rows of stride DP (shared memory).
-// Forward: lane j computes f_ij for every output i, sequentially over k, then the
-// reference gradient g = (label - sigma_table(f)) * alpha * meta (dsgl.hpp:1243-1272),
-// stored transposed: corrT[j * OP + i].  Optional fp32 per-lane loss.
-template <class InPtr>
+// Packed fp32x2 arithmetic (Blackwell FFMA2/FADD2): each half is an ordinary IEEE
+// operation, so pairing two independent sums changes no result.
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 fadd2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+
+// Output-row layout of one step for at most OM outputs (OM = K + 2):
+//   normal rows:      out[i * DP + c]                          (backward, table updates)
+//   interleaved rows: outI[(p * d + c) * 2 + b] = out_{2p+b}[c]   (forward; a float4
+//                     holds the pair (2p, 2p+1) for two consecutive columns)
+//   gradients:        corrP[j * CS + i] = {g_ij, g_ij}          (duplicated pairs)
+template <int OM>
+struct StepShape {
+  static constexpr int OMP = (OM + 1) & ~1;  // outputs rounded up to pairs
+  static constexpr int NPAIR = OMP / 2;
+  static constexpr int CS = OMP + 2;        // corrP row stride in pairs (16-byte rows)
+};
+
+// Forward: lane j computes f_ij for every output i, sequentially over k (pairs of
+// outputs share one FFMA2), then the reference gradient g = (label - sigma_table(f)) *
+// alpha * meta (dsgl.hpp:1243-1272).  Optional fp32 per-lane loss.
+template <int OM, class InPtr>
 __device__ __forceinline__ void forward_gradient(int I, int first, int O, int d, InPtr in_ptr,
-                                                 const float* out_rows, int DP,
-                                                 const int* out_meta, const float* exp_table,
-                                                 float alpha, float* corrT, int OP,
+                                                 const float* outI, const int* out_meta,
+                                                 const float* exp_table, float alpha, float2* corrP,
                                                  bool want_loss, float& loss) {
+  typedef StepShape<OM> SS;
   const int lane = lane_id();
   const int d4 = d >> 2;
   for (int j0 = 0; j0 < I; j0 += 32) {
     const int j = j0 + lane;
     const float4* x = reinterpret_cast<const float4*>(in_ptr(j < I ? j : I - 1));
-    float f[kOMax];
+    float2 f[SS::NPAIR];
 #pragma unroll
-    for (int i = 0; i < kOMax; i++) f[i] = 0.f;
+    for (int q = 0; q < SS::NPAIR; q++) f[q] = make_float2(0.f, 0.f);
     for (int k4 = 0; k4 < d4; k4++) {
       const float4 xv = x[k4];
+      const float2 x0 = make_float2(xv.x, xv.x), x1 = make_float2(xv.y, xv.y);
+      const float2 x2 = make_float2(xv.z, xv.z), x3 = make_float2(xv.w, xv.w);
 #pragma unroll
-      for (int i = 0; i < kOMax; i++) {
-        if (i < O) {
-          const float4 o = reinterpret_cast<const float4*>(out_rows + (size_t)i * DP)[k4];
-          f[i] = __fmaf_rn(o.x, xv.x, f[i]);
-          f[i] = __fmaf_rn(o.y, xv.y, f[i]);
-          f[i] = __fmaf_rn(o.z, xv.z, f[i]);
-          f[i] = __fmaf_rn(o.w, xv.w, f[i]);
+      for (int q = 0; q < SS::NPAIR; q++) {
+        if (2 * q < O) {
+          const float4* op = reinterpret_cast<const float4*>(outI + ((size_t)q * d + 4 * k4) * 2);
+          const float4 a = op[0], b = op[1];
+          f[q] = ffma2(make_float2(a.x, a.y), x0, f[q]);
+          f[q] = ffma2(make_float2(a.z, a.w), x1, f[q]);
+          f[q] = ffma2(make_float2(b.x, b.y), x2, f[q]);
+          f[q] = ffma2(make_float2(b.z, b.w), x3, f[q]);
         }
       }
     }
     if (j < I) {
 #pragma unroll
-      for (int i = 0; i < kOMax; i++) {
+      for (int i = 0; i < OM; i++) {
         if (i < O) {
           const int label = j < first ? (i == 0) : (i == O - 1);
-          const float fi = f[i];
+          const float fi = (i & 1) ? f[i >> 1].y : f[i >> 1].x;
           float g;
           if (fi > (float)kMaxExp) {
             g = __fmul_rn((float)(label - 1), alpha);
@@ -307,7 +311,8 @@ __device__ __forceinline__ void forward_gradient(int I, int first, int O, int d,
                 __float2int_rz(__fmul_rn(__fadd_rn(fi, (float)kMaxExp), (float)kTableScale));
             g = __fmul_rn(__fsub_rn((float)label, exp_table[idx]), alpha);
           }
-          corrT[j * OP + i] = __fmul_rn(g, (float)out_meta[i]);
+          const float gm = __fmul_rn(g, (float)out_meta[i]);
+          corrP[j * SS::CS + i] = make_float2(gm, gm);
           if (want_loss) {  // meta * softplus(-(2 label - 1) f) = -meta log sigma(+-f)
             const float z = label ? -fi : fi;
             loss += (float)out_meta[i] * (fmaxf(z, 0.f) + log1pf(__expf(-fabsf(z))));
@@ -319,66 +324,149 @@ __device__ __forceinline__ void forward_gradient(int I, int first, int O, int d,
   __syncwarp();
 }
 
-// Backward.  Lane owns column chunks q = lane + 32 t (t < DCH, q < d/4).
+// Backward.  Lane owns column chunks q = lane + 32 t (t < DCH, q < d/4), as two pairs.
 //   md[i][t]  = sum_j corr[i][j] * in_j[q]     (outputMd, dsgl.hpp:1290), sequential j
 //   in_j[q]  += sum_i corr[i][j] * out_i[q]     (inputM then buffer +=, dsgl.hpp:1309-1333),
 //               sequential i, inputs applied in order j = 0..I-1.
 // md is complete before any input row changes, as the reference's two GEMMs read the
-// same pre-update inputM.
-// apply_in(j, q, a) consumes input j's update chunk q (the trainers add it to the
-// buffered row in place; the minibatch entry point stores it).
-template <int DCH, class InPtr, class ApplyIn>
+// same pre-update inputM.  apply_in(j, q, a) consumes input j's update of chunk q.
+template <int OM, int DCH, class InPtr, class ApplyIn>
 __device__ __forceinline__ void backward(int I, int O, int d, InPtr in_ptr, const float* out_rows,
-                                         int DP, const float* corrT, int OP,
-                                         float4 (&md)[kOMax][DCH], ApplyIn apply_in) {
+                                         int DP, const float2* corrP, float4 (&md)[OM][DCH],
+                                         ApplyIn apply_in) {
+  typedef StepShape<OM> SS;
   const int lane = lane_id();
   const int d4 = d >> 2;
+  float2 mlo[OM][DCH], mhi[OM][DCH];
 #pragma unroll
-  for (int i = 0; i < kOMax; i++)
+  for (int i = 0; i < OM; i++)
 #pragma unroll
-    for (int t = 0; t < DCH; t++) md[i][t] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int t = 0; t < DCH; t++) mlo[i][t] = mhi[i][t] = make_float2(0.f, 0.f);
   for (int j = 0; j < I; j++) {
     const float4* x = reinterpret_cast<const float4*>(in_ptr(j));
-    float c[kOMax];
+    const float4* cj = reinterpret_cast<const float4*>(corrP + j * SS::CS);
+    float2 c[SS::OMP];
 #pragma unroll
-    for (int i = 0; i < kOMax; i++) c[i] = i < O ? corrT[j * OP + i] : 0.f;
+    for (int q = 0; q < SS::NPAIR; q++) {
+      const float4 v = cj[q];
+      c[2 * q] = make_float2(v.x, v.y);
+      c[2 * q + 1] = make_float2(v.z, v.w);
+    }
 #pragma unroll
     for (int t = 0; t < DCH; t++) {
       const int q = lane + 32 * t;
       if (q < d4) {
         const float4 xv = x[q];
+        const float2 xl = make_float2(xv.x, xv.y), xh = make_float2(xv.z, xv.w);
 #pragma unroll
-        for (int i = 0; i < kOMax; i++)
-          if (i < O) md[i][t] = fma4s(c[i], xv, md[i][t]);
+        for (int i = 0; i < OM; i++)
+          if (i < O) {
+            mlo[i][t] = ffma2(c[i], xl, mlo[i][t]);
+            mhi[i][t] = ffma2(c[i], xh, mhi[i][t]);
+          }
       }
     }
   }
-  float4 o[kOMax][DCH];
 #pragma unroll
-  for (int i = 0; i < kOMax; i++)
+  for (int i = 0; i < OM; i++)
+#pragma unroll
+    for (int t = 0; t < DCH; t++) md[i][t] = make_float4(mlo[i][t].x, mlo[i][t].y, mhi[i][t].x, mhi[i][t].y);
+  float2 olo[OM][DCH], ohi[OM][DCH];
+#pragma unroll
+  for (int i = 0; i < OM; i++)
 #pragma unroll
     for (int t = 0; t < DCH; t++) {
       const int q = lane + 32 * t;
-      o[i][t] = (i < O && q < d4) ? reinterpret_cast<const float4*>(out_rows + (size_t)i * DP)[q]
-                                  : make_float4(0.f, 0.f, 0.f, 0.f);
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (i < O && q < d4) v = reinterpret_cast<const float4*>(out_rows + (size_t)i * DP)[q];
+      olo[i][t] = make_float2(v.x, v.y);
+      ohi[i][t] = make_float2(v.z, v.w);
     }
   for (int j = 0; j < I; j++) {
-    float c[kOMax];
+    const float4* cj = reinterpret_cast<const float4*>(corrP + j * SS::CS);
+    float2 c[SS::OMP];
 #pragma unroll
-    for (int i = 0; i < kOMax; i++) c[i] = i < O ? corrT[j * OP + i] : 0.f;
+    for (int q = 0; q < SS::NPAIR; q++) {
+      const float4 v = cj[q];
+      c[2 * q] = make_float2(v.x, v.y);
+      c[2 * q + 1] = make_float2(v.z, v.w);
+    }
 #pragma unroll
     for (int t = 0; t < DCH; t++) {
       const int q = lane + 32 * t;
       if (q < d4) {
-        float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+        float2 al = make_float2(0.f, 0.f), ah = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int i = 0; i < kOMax; i++)
-          if (i < O) a = fma4s(c[i], o[i][t], a);
-        apply_in(j, q, a);
+        for (int i = 0; i < OM; i++)
+          if (i < O) {
+            al = ffma2(c[i], olo[i][t], al);
+            ah = ffma2(c[i], ohi[i][t], ah);
+          }
+        apply_in(j, q, make_float4(al.x, al.y, ah.x, ah.y));
       }
     }
   }
   __syncwarp();
+}
+
+// Stores the step's output rows from registers in both layouts (see StepShape).
+template <int OM, int DCH>
+__device__ __forceinline__ void store_out_rows(const float4 (&v)[OM][DCH], int O, int d, float* out_rows,
+                                               int DP, float* outI) {
+  typedef StepShape<OM> SS;
+  const int lane = lane_id(), d4 = d >> 2;
+#pragma unroll
+  for (int t = 0; t < DCH; t++) {
+    const int q = lane + 32 * t;
+    if (q < d4) {
+#pragma unroll
+      for (int i = 0; i < OM; i++)
+        if (i < O) reinterpret_cast<float4*>(out_rows + (size_t)i * DP)[q] = v[i][t];
+#pragma unroll
+      for (int p = 0; p < SS::NPAIR; p++) {
+        if (2 * p < O) {
+          const float4 a = v[2 * p][t];
+          const float4 b = (2 * p + 1 < O) ? v[2 * p + 1][t] : make_float4(0.f, 0.f, 0.f, 0.f);
+          float4* dst = reinterpret_cast<float4*>(outI + ((size_t)p * d + 4 * q) * 2);
+          dst[0] = make_float4(a.x, b.x, a.y, b.y);
+          dst[1] = make_float4(a.z, b.z, a.w, b.w);
+        }
+      }
+    }
+  }
+}
+
+// trainers: buffered input row += update
+template <class InPtr>
+struct AddToInput {
+  InPtr in_ptr;
+  __device__ __forceinline__ void operator()(int j, int q, float4 a) const {
+    float4* x = reinterpret_cast<float4*>(const_cast<float*>(in_ptr(j)));
+    const float4 v = x[q];
+    const float2 lo = fadd2(make_float2(v.x, v.y), make_float2(a.x, a.y));
+    const float2 hi = fadd2(make_float2(v.z, v.w), make_float2(a.z, a.w));
+    x[q] = make_float4(lo.x, lo.y, hi.x, hi.y);
+  }
+};
+template <class InPtr>
+__device__ __forceinline__ AddToInput<InPtr> add_to_input(InPtr f) {
+  return AddToInput<InPtr>{f};
+}
+
+// Loads the step's output rows (all loads in flight before any use) into registers.
+template <int S, int OM, int DCH>
+__device__ __forceinline__ void load_out_rows(const void* tab, const int* ids, int O, int d,
+                                              float4 (&v)[OM][DCH]) {
+  const int lane = lane_id(), d4 = d >> 2;
+#pragma unroll
+  for (int i = 0; i < OM; i++) {
+    const int row = i < O ? ids[i] : 0;
+#pragma unroll
+    for (int t = 0; t < DCH; t++) {
+      const int q = lane + 32 * t;
+      v[i][t] = (i < O && q < d4) ? RowIO<S>::load4(tab, row, d, q) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
 }
 
 }  // namespace sgns

@@ -61,10 +61,12 @@ __host__ __device__ inline PlainLayout plain_layout(int d, int K, int lmax) {
 
 constexpr int kPlainWarps = 4;
 
-// per-warp shared memory (words): output rows, corrT, input offsets, output ids/meta/draw
+// per-warp shared memory (words): output rows, interleaved output rows, gradient pairs,
+// input offsets, output ids/meta/draw index (kOMax outputs)
 __host__ __device__ inline size_t plain_warp_words(int d, int w, int K) {
-  const int DP = d + 4, OP = (K + 2 + 3) & ~3;
-  return align_up((size_t)(K + 2) * DP + (size_t)4 * w * OP + 4 * w + 3 * (K + 2), 4);
+  (void)K;
+  const int DP = d + 4;
+  return align_up((size_t)kOMax * DP + (size_t)kOMax * d + (size_t)4 * w * (kOMax + 2) * 2 + 4 * w + 3 * kOMax, 4);
 }
 
 template <int S>
@@ -133,14 +135,15 @@ __global__ void __launch_bounds__(32 * kPlainWarps) plain_step_kernel(TrainParam
   if (wid >= p.workers) return;
 
   const int d = p.d, w = p.window, K = p.K, lmax = p.lmax;
-  const int DP = d + 4, OP = (K + 2 + 3) & ~3;
+  const int DP = d + 4;
   float* wsm = smem + 1136 + (size_t)(threadIdx.x >> 5) * plain_warp_words(d, w, K);
   float* out_rows = wsm;
-  float* corrT = out_rows + (size_t)(K + 2) * DP;
-  int* in_off = reinterpret_cast<int*>(corrT + 4 * w * OP);
+  float* outI = out_rows + (size_t)kOMax * DP;
+  float2* corrP = reinterpret_cast<float2*>(outI + (size_t)kOMax * d);
+  int* in_off = reinterpret_cast<int*>(corrP + (size_t)4 * w * (kOMax + 2));
   int* out_id = in_off + 4 * w;
-  int* out_meta = out_id + (K + 2);
-  int* kidx = out_meta + (K + 2);
+  int* out_meta = out_id + kOMax;
+  int* kidx = out_meta + kOMax;
 
   const PlainLayout L = plain_layout(d, K, lmax);
   char* scr = static_cast<char*>(p.plain_state) + (size_t)wid * (size_t)p.plain_stride;
@@ -241,26 +244,30 @@ __global__ void __launch_bounds__(32 * kPlainWarps) plain_step_kernel(TrainParam
     st.neg_count++;
     const int g = st.neg_count % st.neg_n;
     const int O = select_outputs_stored(K, negw + (size_t)g * K, t1, t2, out_id, out_meta, kidx);
-    {
+    {  // outputs: targets from Woh (global), negatives from the pool buffer
+      float4 v[kOMax][DCH];
       const int d4 = d >> 2;
-      for (int i = 0; i < O; i++) {
-        float4* dst = reinterpret_cast<float4*>(out_rows + (size_t)i * DP);
-        if (i == 0 || i == O - 1) {
-          const int row = out_id[i];
-          for (int q = lane; q < d4; q += 32) dst[q] = RowIO<S>::load4(p.woh, row, d, q);
-        } else {
-          const float4* src = reinterpret_cast<const float4*>(negbuf + (size_t)negslot[g * K + kidx[i]] * d);
-          for (int q = lane; q < d4; q += 32) dst[q] = src[q];
+#pragma unroll
+      for (int i = 0; i < kOMax; i++)
+#pragma unroll
+        for (int t = 0; t < DCH; t++) {
+          const int q = lane + 32 * t;
+          float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (i < O && q < d4) {
+            if (i == 0 || i == O - 1) x = RowIO<S>::load4(p.woh, out_id[i], d, q);
+            else x = reinterpret_cast<const float4*>(negbuf + (size_t)negslot[g * K + kidx[i]] * d)[q];
+          }
+          v[i][t] = x;
         }
-      }
+      store_out_rows<kOMax, DCH>(v, O, d, out_rows, DP, outI);
     }
     __syncwarp();
     const float alpha = *reinterpret_cast<volatile float*>(&p.ctr->alpha);
     auto in_ptr = [&](int j) -> const float* { return buf + (size_t)in_off[j] * d; };
-    forward_gradient(I, I0, O, d, in_ptr, out_rows, DP, out_meta, exp_s, alpha, corrT, OP,
-                     p.compute_loss != 0, loss);
+    forward_gradient<kOMax>(I, I0, O, d, in_ptr, outI, out_meta, exp_s, alpha, corrP, p.compute_loss != 0,
+                            loss);
     float4 md[kOMax][DCH];
-    backward<DCH>(I, O, d, in_ptr, out_rows, DP, corrT, OP, md, add_to_input(in_ptr));
+    backward<kOMax, DCH>(I, O, d, in_ptr, out_rows, DP, corrP, md, add_to_input(in_ptr));
     {
       uint64_t e1 = 0, e2 = 0;
       if (S == STORE_BF16) {

@@ -26,7 +26,7 @@ namespace {
 constexpr int kHdrWords = 1004 + 132;  // sigmoid table (1001 -> 1004) + SmallJumps (528 B)
 
 struct WinLayout {  // per-warp shared memory, in 4-byte words
-  int NS, R, DP, OP, OM, IM, lmax;
+  int NS, R, DP, OP, OM, IM, lmax, outI;
   int rows, corr, sen, vert, ref, ring, inrow, outid, outmeta, pend, words;
 };
 
@@ -35,15 +35,17 @@ __host__ __device__ inline WinLayout win_layout(int d, int w, int K, int lmax) {
   L.NS = 2 * w + 2;  // resident slots per walk (2w+1 positions, +1 while a row enters)
   L.R = 2 * w + 2;   // ring of position -> slot
   L.DP = d + 4;      // padded row stride: 32 lanes reading 32 rows hit 32 distinct banks
-  L.OM = K + 2;
-  L.OP = (L.OM + 3) & ~3;
+  L.OM = K <= 5 ? 7 : kOMax;  // the kernel variant's output capacity (K + 2 <= OM)
+  L.OP = (L.OM + 1) & ~1;     // outputs rounded up to pairs
   L.IM = 4 * w;
   L.lmax = lmax;
   int off = 0;
   L.rows = off;
   off += (2 * L.NS + L.OM) * L.DP;
-  L.corr = off;
-  off += L.IM * L.OP;
+  L.outI = off;  // interleaved output rows (forward operand)
+  off += L.OP * d;
+  L.corr = off;  // duplicated gradient pairs, stride OP + 2 pairs per input
+  off += L.IM * (L.OP + 2) * 2;
   L.sen = off;
   off += 2 * lmax;
   L.vert = off;
@@ -110,7 +112,7 @@ __device__ __forceinline__ void store_row_from_smem(void* tab, int64_t row, int 
     RowIO<S>::store4(tab, row, d, q, reinterpret_cast<const float4*>(src)[q], ev);
 }
 
-template <int S, int DCH>
+template <int S, int DCH, int OM>
 __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
   extern __shared__ __align__(16) float smem[];
   float* exp_s = smem;
@@ -131,7 +133,8 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
   float* base = smem + kHdrWords + (threadIdx.x >> 5) * L.words;
   float* rows = base + L.rows;
   float* out_rows = rows + (size_t)2 * L.NS * L.DP;
-  float* corrT = base + L.corr;
+  float* outI = base + L.outI;
+  float2* corrP = reinterpret_cast<float2*>(base + L.corr);
   int* sen = reinterpret_cast<int*>(base + L.sen);
   int* vert = reinterpret_cast<int*>(base + L.vert);
   int* ref = reinterpret_cast<int*>(base + L.ref);
@@ -291,15 +294,17 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     grp_g = g;
     grp_state = gs;
     const int O = select_outputs(p, *sj, gs, t1, t2, out_id, out_meta);
-    // gather the output rows (targets and negatives) from Woh, all loads in flight at once
-    load_rows_batched<S, DCH, (DCH == 1 ? kOMax : 4)>(p.woh, out_id, O, d, [&](int u) { return out_rows + (size_t)u * DP; });
+    {  // gather the output rows (targets and negatives) from Woh, all loads in flight at once
+      float4 v[OM][DCH];
+      load_out_rows<S, OM, DCH>(p.woh, out_id, O, d, v);
+      store_out_rows<OM, DCH>(v, O, d, out_rows, DP, outI);
+    }
     __syncwarp();
     const float alpha = *reinterpret_cast<volatile float*>(&p.ctr->alpha);
     auto in_ptr = [&](int j) -> const float* { return rows + (size_t)in_row[j] * DP; };
-    forward_gradient(I, I0, O, d, in_ptr, out_rows, DP, out_meta, exp_s, alpha, corrT, L.OP,
-                     p.compute_loss != 0, loss);
-    float4 md[kOMax][DCH];
-    backward<DCH>(I, O, d, in_ptr, out_rows, DP, corrT, L.OP, md, add_to_input(in_ptr));
+    forward_gradient<OM>(I, I0, O, d, in_ptr, outI, out_meta, exp_s, alpha, corrP, p.compute_loss != 0, loss);
+    float4 md[OM][DCH];
+    backward<OM, DCH>(I, O, d, in_ptr, out_rows, DP, corrP, md, add_to_input(in_ptr));
     {  // Woh += outputMd: target 1, target 2, then each negative (aliases follow that order)
       uint64_t e1 = 0, e2 = 0, en = 0;
       if (S == STORE_BF16) {
@@ -313,16 +318,16 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
         const int q = lane + 32 * t;
         if (q < d4) {
           float4 mlast = md[0][t];
+          float4 blast = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-          for (int i = 1; i < kOMax; i++)
+          for (int i = 1; i < OM; i++)
             if (i == O - 1) mlast = md[i][t];
           const float4 b1 = reinterpret_cast<const float4*>(out_rows)[q];
           const float4 n1 = RowIO<S>::store4(p.woh, t1, d, q, add4(b1, md[0][t]), e1);
-          const float4 b2 = t2 == t1 ? n1
-                                     : reinterpret_cast<const float4*>(out_rows + (size_t)(O - 1) * DP)[q];
-          const float4 n2 = RowIO<S>::store4(p.woh, t2, d, q, add4(b2, mlast), e2);
+          blast = t2 == t1 ? n1 : reinterpret_cast<const float4*>(out_rows + (size_t)(O - 1) * DP)[q];
+          const float4 n2 = RowIO<S>::store4(p.woh, t2, d, q, add4(blast, mlast), e2);
 #pragma unroll
-          for (int i = 1; i < kOMax - 1; i++) {
+          for (int i = 1; i < OM - 1; i++) {
             if (i < O - 1) {
               const int row = out_id[i];
               const float4 bi = row == t2 ? n2
@@ -416,37 +421,46 @@ size_t window_smem_bytes(int d, int window, int K, int lmax, int warps_per_cta) 
   return sizeof(float) * ((size_t)kHdrWords + (size_t)warps_per_cta * L.words);
 }
 
-template <int S, int DCH>
+template <int S, int DCH, int OM>
 static cudaError_t occupancy_t(int d, int w, int K, int lmax, int wpc, int* ctas) {
   const size_t smem = window_smem_bytes(d, w, K, lmax, wpc);
-  cudaError_t e = cudaFuncSetAttribute(window_engine_kernel<S, DCH>,
+  cudaError_t e = cudaFuncSetAttribute(window_engine_kernel<S, DCH, OM>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas, window_engine_kernel<S, DCH>, 32 * wpc, smem);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas, window_engine_kernel<S, DCH, OM>, 32 * wpc, smem);
 }
 
-cudaError_t window_engine_occupancy(int storage, int d, int w, int K, int lmax, int wpc, int* ctas) {
-  const bool wide = d > 128;
-  if (storage == STORE_BF16)
-    return wide ? occupancy_t<STORE_BF16, 2>(d, w, K, lmax, wpc, ctas) : occupancy_t<STORE_BF16, 1>(d, w, K, lmax, wpc, ctas);
-  return wide ? occupancy_t<STORE_F32, 2>(d, w, K, lmax, wpc, ctas) : occupancy_t<STORE_F32, 1>(d, w, K, lmax, wpc, ctas);
-}
-
-template <int S, int DCH>
+template <int S, int DCH, int OM>
 static cudaError_t launch_t(const TrainParams& p, int wpc, cudaStream_t s) {
   const size_t smem = window_smem_bytes(p.d, p.window, p.K, p.lmax, wpc);
-  cudaError_t e = cudaFuncSetAttribute(window_engine_kernel<S, DCH>,
+  cudaError_t e = cudaFuncSetAttribute(window_engine_kernel<S, DCH, OM>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const int blocks = (p.workers + wpc - 1) / wpc;
-  window_engine_kernel<S, DCH><<<blocks, 32 * wpc, smem, s>>>(p);
+  window_engine_kernel<S, DCH, OM><<<blocks, 32 * wpc, smem, s>>>(p);
   return cudaGetLastError();
 }
 
+// kernel variants: storage x column chunks per lane (d <= 128 or <= 256) x outputs per
+// step (K <= 5 or K <= 10)
+#define SGNS_WINDOW_DISPATCH(FN, ...)                                                         \
+  do {                                                                                     \
+    const bool wide_ = d > 128, small_ = K <= 5;                                           \
+    if (storage == STORE_BF16) {                                                           \
+      if (wide_) return small_ ? FN<STORE_BF16, 2, 7>(__VA_ARGS__) : FN<STORE_BF16, 2, kOMax>(__VA_ARGS__); \
+      return small_ ? FN<STORE_BF16, 1, 7>(__VA_ARGS__) : FN<STORE_BF16, 1, kOMax>(__VA_ARGS__);            \
+    }                                                                                      \
+    if (wide_) return small_ ? FN<STORE_F32, 2, 7>(__VA_ARGS__) : FN<STORE_F32, 2, kOMax>(__VA_ARGS__);     \
+    return small_ ? FN<STORE_F32, 1, 7>(__VA_ARGS__) : FN<STORE_F32, 1, kOMax>(__VA_ARGS__);                \
+  } while (0)
+
+cudaError_t window_engine_occupancy(int storage, int d, int w, int K, int lmax, int wpc, int* ctas) {
+  SGNS_WINDOW_DISPATCH(occupancy_t, d, w, K, lmax, wpc, ctas);
+}
+
 cudaError_t launch_window_engine(const TrainParams& p, int wpc, cudaStream_t s) {
-  const bool wide = p.d > 128;
-  if (p.storage == STORE_BF16) return wide ? launch_t<STORE_BF16, 2>(p, wpc, s) : launch_t<STORE_BF16, 1>(p, wpc, s);
-  return wide ? launch_t<STORE_F32, 2>(p, wpc, s) : launch_t<STORE_F32, 1>(p, wpc, s);
+  const int d = p.d, K = p.K, storage = p.storage;
+  SGNS_WINDOW_DISPATCH(launch_t, p, wpc, s);
 }
 
 }  // namespace sgns
