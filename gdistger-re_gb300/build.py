@@ -55,7 +55,8 @@ def build(verbose_ptxas=False, force=False):
         o = os.path.join(OUT, src + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append([NVCC, "-O2", "-std=c++17", "-Xcompiler", "-fPIC,-Wall", "-c", s, "-o", o])
+            jobs.append([NVCC, "-O2", "-std=c++17", "-Xcompiler", "-fPIC,-Wall", "-I", os.path.join(ROOT, "include"),
+                         "-c", s, "-o", o])
     logs = []
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for out in ex.map(_run, jobs):

@@ -21,7 +21,7 @@
 #include <thread>
 #include <vector>
 
-#include "../../include/sgns.h"
+#include "sgns.h"
 #include "sgns_internal.h"
 
 using namespace sgns;
