@@ -324,6 +324,75 @@ __device__ __forceinline__ void forward_gradient(int I, int first, int O, int d,
   __syncwarp();
 }
 
+// Forward of the persistent engine: the same gradient, with each dot product summed as
+// four independent sequential quarter-sums over k combined as (s0 + s1) + (s2 + s3)
+// (d % 16 == 0).  Sixteen independent FFMA2 chains per lane instead of four 4x longer
+// ones; the oracle's window policy uses the same order.
+template <int OM, class InPtr>
+__device__ __forceinline__ void forward_gradient_split4(int I, int first, int O, int d, InPtr in_ptr,
+                                                        const float* outI, const int* out_meta,
+                                                        const float* exp_table, float alpha, float2* corrP,
+                                                        bool want_loss, float& loss) {
+  typedef StepShape<OM> SS;
+  const int lane = lane_id();
+  const int q4 = d >> 4;  // chunks of 4 columns per quarter
+  for (int j0 = 0; j0 < I; j0 += 32) {
+    const int j = j0 + lane;
+    const float4* x = reinterpret_cast<const float4*>(in_ptr(j < I ? j : I - 1));
+    float2 f[SS::NPAIR][4];
+#pragma unroll
+    for (int q = 0; q < SS::NPAIR; q++)
+#pragma unroll
+      for (int m = 0; m < 4; m++) f[q][m] = make_float2(0.f, 0.f);
+    for (int k4 = 0; k4 < q4; k4++) {
+      float4 xv[4];
+#pragma unroll
+      for (int m = 0; m < 4; m++) xv[m] = x[m * q4 + k4];
+#pragma unroll
+      for (int q = 0; q < SS::NPAIR; q++) {
+        if (2 * q < O) {
+#pragma unroll
+          for (int m = 0; m < 4; m++) {
+            const float4* op = reinterpret_cast<const float4*>(outI + ((size_t)q * d + 4 * (m * q4 + k4)) * 2);
+            const float4 a = op[0], b = op[1];
+            f[q][m] = ffma2(make_float2(a.x, a.y), make_float2(xv[m].x, xv[m].x), f[q][m]);
+            f[q][m] = ffma2(make_float2(a.z, a.w), make_float2(xv[m].y, xv[m].y), f[q][m]);
+            f[q][m] = ffma2(make_float2(b.x, b.y), make_float2(xv[m].z, xv[m].z), f[q][m]);
+            f[q][m] = ffma2(make_float2(b.z, b.w), make_float2(xv[m].w, xv[m].w), f[q][m]);
+          }
+        }
+      }
+    }
+    if (j < I) {
+#pragma unroll
+      for (int i = 0; i < OM; i++) {
+        if (i < O) {
+          const int label = j < first ? (i == 0) : (i == O - 1);
+          const float2 s = fadd2(fadd2(f[i >> 1][0], f[i >> 1][1]), fadd2(f[i >> 1][2], f[i >> 1][3]));
+          const float fi = (i & 1) ? s.y : s.x;
+          float g;
+          if (fi > (float)kMaxExp) {
+            g = __fmul_rn((float)(label - 1), alpha);
+          } else if (fi < -(float)kMaxExp) {
+            g = __fmul_rn((float)label, alpha);
+          } else {
+            const int idx =
+                __float2int_rz(__fmul_rn(__fadd_rn(fi, (float)kMaxExp), (float)kTableScale));
+            g = __fmul_rn(__fsub_rn((float)label, exp_table[idx]), alpha);
+          }
+          const float gm = __fmul_rn(g, (float)out_meta[i]);
+          corrP[j * SS::CS + i] = make_float2(gm, gm);
+          if (want_loss) {
+            const float z = label ? -fi : fi;
+            loss += (float)out_meta[i] * (fmaxf(z, 0.f) + log1pf(__expf(-fabsf(z))));
+          }
+        }
+      }
+    }
+  }
+  __syncwarp();
+}
+
 // Backward.  Lane owns column chunks q = lane + 32 t (t < DCH, q < d/4), as two pairs.
 //   md[i][t]  = sum_j corr[i][j] * in_j[q]     (outputMd, dsgl.hpp:1290), sequential j
 //   in_j[q]  += sum_i corr[i][j] * out_i[q]     (inputM then buffer +=, dsgl.hpp:1309-1333),
@@ -382,27 +451,39 @@ __device__ __forceinline__ void backward(int I, int O, int d, InPtr in_ptr, cons
       olo[i][t] = make_float2(v.x, v.y);
       ohi[i][t] = make_float2(v.z, v.w);
     }
-  for (int j = 0; j < I; j++) {
-    const float4* cj = reinterpret_cast<const float4*>(corrP + j * SS::CS);
-    float2 c[SS::OMP];
+  // four inputs per iteration: eight independent chains; updates applied in input order
+  for (int j0 = 0; j0 < I; j0 += 4) {
+    float2 c[4][SS::OMP];
 #pragma unroll
-    for (int q = 0; q < SS::NPAIR; q++) {
-      const float4 v = cj[q];
-      c[2 * q] = make_float2(v.x, v.y);
-      c[2 * q + 1] = make_float2(v.z, v.w);
+    for (int u = 0; u < 4; u++) {
+      const int j = j0 + u < I ? j0 + u : I - 1;
+      const float4* cj = reinterpret_cast<const float4*>(corrP + j * SS::CS);
+#pragma unroll
+      for (int q = 0; q < SS::NPAIR; q++) {
+        const float4 v = cj[q];
+        c[u][2 * q] = make_float2(v.x, v.y);
+        c[u][2 * q + 1] = make_float2(v.z, v.w);
+      }
     }
 #pragma unroll
     for (int t = 0; t < DCH; t++) {
       const int q = lane + 32 * t;
       if (q < d4) {
-        float2 al = make_float2(0.f, 0.f), ah = make_float2(0.f, 0.f);
+        float2 al[4], ah[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) al[u] = ah[u] = make_float2(0.f, 0.f);
 #pragma unroll
         for (int i = 0; i < OM; i++)
           if (i < O) {
-            al = ffma2(c[i], olo[i][t], al);
-            ah = ffma2(c[i], ohi[i][t], ah);
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+              al[u] = ffma2(c[u][i], olo[i][t], al[u]);
+              ah[u] = ffma2(c[u][i], ohi[i][t], ah[u]);
+            }
           }
-        apply_in(j, q, make_float4(al.x, al.y, ah.x, ah.y));
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+          if (j0 + u < I) apply_in(j0 + u, q, make_float4(al[u].x, al[u].y, ah[u].x, ah[u].y));
       }
     }
   }

@@ -11,7 +11,9 @@
 //     written back (stochastically rounded for bf16 tables) when it leaves it,
 //   * the step's output rows (target of each walk + shared negatives) and gradients.
 // Negative rows are read from and added to Woh at each step, as the reference does for
-// the two target rows (dsgl.hpp:1346-1356).  The negative pool keeps the reference's
+// the two target rows (dsgl.hpp:1346-1356).  Dot products of the forward are summed as
+// four sequential quarter-sums combined pairwise (when d % 16 == 0); the backward keeps
+// the reference's order.  The negative pool keeps the reference's
 // draw stream (max(len1,len2)*K draws per pool, group neg_count % n per step,
 // dsgl.hpp:1054-1073, 1136-1154) but is regenerated from its base LCG state instead of
 // being stored.
@@ -302,7 +304,11 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     __syncwarp();
     const float alpha = *reinterpret_cast<volatile float*>(&p.ctr->alpha);
     auto in_ptr = [&](int j) -> const float* { return rows + (size_t)in_row[j] * DP; };
-    forward_gradient<OM>(I, I0, O, d, in_ptr, outI, out_meta, exp_s, alpha, corrP, p.compute_loss != 0, loss);
+    if ((d & 15) == 0)
+      forward_gradient_split4<OM>(I, I0, O, d, in_ptr, outI, out_meta, exp_s, alpha, corrP, p.compute_loss != 0,
+                                  loss);
+    else
+      forward_gradient<OM>(I, I0, O, d, in_ptr, outI, out_meta, exp_s, alpha, corrP, p.compute_loss != 0, loss);
     float4 md[OM][DCH];
     backward<OM, DCH>(I, O, d, in_ptr, out_rows, DP, corrP, md, add_to_input(in_ptr));
     {  // Woh += outputMd: target 1, target 2, then each negative (aliases follow that order)

@@ -26,7 +26,9 @@
 //                    rows are held on chip while any of their positions lies in the
 //                    sliding window [pos-w, pos+w] (one copy per walk, exactly as the
 //                    reference dedupes them) and written back when they leave it;
-//                    negative rows are read from and added to Woh at each step.
+//                    negative rows are read from and added to Woh at each step; each
+//                    forward dot product is four sequential quarter-sums combined
+//                    pairwise (d % 16 == 0).
 // Storage: FP32, BF16 with stochastic rounding on every write-back, or FP64.
 #include <algorithm>
 #include <atomic>
@@ -460,13 +462,26 @@ struct Worker {
 
     // forward + gradient (dsgl.hpp:1241-1272, MKL branch labels)
     const A alpha = (A)sh.alpha.load(std::memory_order_relaxed);
+    // The window policy's engine sums each dot product as four sequential quarter-sums
+    // combined as (s0 + s1) + (s2 + s3) when d % 16 == 0; the reference order otherwise.
+    const bool split4 = sh.policy == POLICY_WINDOW && d % 16 == 0;
     for (int i = 0; i < O; i++) {
       const A c = (A)out_meta[i];
       for (int j = 0; j < I; j++) {
         A f = 0;
         const A* o = &outputM[(size_t)i * d];
         const A* x = &inputM[(size_t)j * d];
-        for (int k = 0; k < d; k++) f = fma_acc(o[k], x[k], f);
+        if (split4) {
+          const int qd = d / 4;
+          A s4[4];
+          for (int m = 0; m < 4; m++) {
+            s4[m] = 0;
+            for (int k = m * qd; k < (m + 1) * qd; k++) s4[m] = fma_acc(o[k], x[k], s4[m]);
+          }
+          f = (s4[0] + s4[1]) + (s4[2] + s4[3]);
+        } else {
+          for (int k = 0; k < d; k++) f = fma_acc(o[k], x[k], f);
+        }
         int label = j < first ? (i == 0 ? 1 : 0) : (i == O - 1 ? 1 : 0);
         A g;
         if (f > kMaxExp) g = (A)(label - 1) * alpha;
