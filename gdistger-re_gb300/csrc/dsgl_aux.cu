@@ -62,8 +62,7 @@ __global__ void __launch_bounds__(32) minibatch_kernel(int d, int imax, int omax
   const int DP = d + 4;
   float* exp_s = smem;
   float* xin = smem + 1004;
-  float* xout = xin + (size_t)imax * DP;
-  float* outI = xout + (size_t)kOMax * DP;
+  float* outI = xin + (size_t)imax * DP;
   float2* corrP = reinterpret_cast<float2*>(outI + (size_t)kOMax * d);
   int* meta = reinterpret_cast<int*>(corrP + (size_t)imax * (kOMax + 2));
   for (int i = lane; i < kExpTableSize + 1; i += 32) exp_s[i] = exp_table[i];
@@ -83,7 +82,7 @@ __global__ void __launch_bounds__(32) minibatch_kernel(int d, int imax, int omax
         v[i][t] = (i < O && q < d4) ? reinterpret_cast<const float4*>(gout + (size_t)i * d)[q]
                                     : make_float4(0.f, 0.f, 0.f, 0.f);
       }
-    store_out_rows<kOMax, DCH>(v, O, d, xout, DP, outI);
+    store_out_interleaved<kOMax, DCH>(v, O, d, outI);
   }
   for (int i = lane; i < O; i += 32) meta[i] = out_meta_all[out_off[b] + i];
   __syncwarp();
@@ -92,7 +91,7 @@ __global__ void __launch_bounds__(32) minibatch_kernel(int d, int imax, int omax
   forward_gradient<kOMax>(I, first, O, d, in_ptr, outI, meta, exp_s, alpha[b], corrP, false, loss);
   float4 md[kOMax][DCH];
   float* gdin = d_in + in_off[b] * d;
-  backward<kOMax, DCH>(I, O, d, in_ptr, xout, DP, corrP, md,
+  backward<kOMax, DCH>(I, O, d, in_ptr, outI, corrP, md,
                        [&](int j, int q, float4 a) { reinterpret_cast<float4*>(gdin + (size_t)j * d)[q] = a; });
   float* gdout = d_out + out_off[b] * d;
 #pragma unroll
@@ -166,7 +165,7 @@ cudaError_t launch_minibatch(int d, int n, int imax, int omax, const int32_t* in
   prefix_offsets_kernel<<<1, 1, 0, s>>>(in_count, out_count, n, in_off, out_off);
   const int DP = d + 4;
   (void)omax;
-  const size_t smem = sizeof(float) * (1004 + (size_t)(imax + kOMax) * DP + (size_t)kOMax * d +
+  const size_t smem = sizeof(float) * (1004 + (size_t)imax * DP + (size_t)kOMax * d +
                                        (size_t)imax * (kOMax + 2) * 2 + kOMax + 4);
   cudaError_t e;
   if (d > 128) {

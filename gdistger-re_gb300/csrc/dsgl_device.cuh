@@ -165,20 +165,30 @@ __device__ __forceinline__ int fill_walk(const TrainParams& p, const SmallJumps&
 }
 
 // ---- one group of negatives and the output list (dsgl.hpp:1136-1159) ---------------
-// gstate: LCG state before the group's first draw.  Lanes < K draw; equal draws merge
-// (meta = multiplicity, first occurrence keeps its place); draws equal to t1 are dropped.
-// Writes out_id/out_meta[0..O) in the reference's order; returns O.
-__device__ __forceinline__ int select_outputs(const TrainParams& p, const SmallJumps& sj,
-                                              uint64_t gstate, int t1, int t2, int* out_id,
+// Draw k of the group starting at LCG state gstate is made by lane k: its state and
+// the table entry it indexes (a global load that may be issued a step ahead).
+struct NegDraw {
+  uint64_t st;
+  int raw;
+};
+__device__ __forceinline__ NegDraw neg_draw_issue(const TrainParams& p, const SmallJumps& sj, uint64_t gstate) {
+  NegDraw n;
+  n.st = 0;
+  n.raw = 0;
+  if (lane_id() < p.K) {
+    n.st = jump_small(gstate, lane_id() + 1, sj);
+    n.raw = __ldg(&p.table[fast_mod(n.st >> 16, p.div_table)]);
+  }
+  return n;
+}
+// Equal draws merge (meta = multiplicity, first occurrence keeps its place); draws equal
+// to t1 are dropped.  Writes out_id/out_meta[0..O) in the reference's order; returns O.
+__device__ __forceinline__ int select_outputs(const TrainParams& p, NegDraw nd, int t1, int t2, int* out_id,
                                               int* out_meta) {
   const int lane = lane_id();
   const bool valid = lane < p.K;
   int s = -2 - lane;
-  if (valid) {
-    uint64_t st = jump_small(gstate, lane + 1, sj);
-    s = __ldg(&p.table[fast_mod(st >> 16, p.div_table)]);
-    if (!s) s = (int)(fast_mod(st, p.div_vm1) + 1);
-  }
+  if (valid) s = nd.raw ? nd.raw : (int)(fast_mod(nd.st, p.div_vm1) + 1);
   const unsigned same = __match_any_sync(kFull, s);
   const bool leader = (__ffs(same) - 1) == lane;
   const unsigned distinct = __ballot_sync(kFull, valid && leader && s != t1);
@@ -261,6 +271,14 @@ struct StepShape {
   static constexpr int NPAIR = OMP / 2;
   static constexpr int CS = OMP + 2;        // corrP row stride in pairs (16-byte rows)
 };
+
+// Rows 2p and 2p+1, columns 4q..4q+3, read back from the interleaved layout.
+__device__ __forceinline__ void out_chunk_pair(const float* outI, int d, int p, int q, float4& r0, float4& r1) {
+  const float4* src = reinterpret_cast<const float4*>(outI + ((size_t)p * d + 4 * q) * 2);
+  const float4 a = src[0], b = src[1];
+  r0 = make_float4(a.x, a.z, b.x, b.z);
+  r1 = make_float4(a.y, a.w, b.y, b.w);
+}
 
 // Forward: lane j computes f_ij for every output i, sequentially over k (pairs of
 // outputs share one FFMA2), then the reference gradient g = (label - sigma_table(f)) *
@@ -400,9 +418,8 @@ __device__ __forceinline__ void forward_gradient_split4(int I, int first, int O,
 // md is complete before any input row changes, as the reference's two GEMMs read the
 // same pre-update inputM.  apply_in(j, q, a) consumes input j's update of chunk q.
 template <int OM, int DCH, class InPtr, class ApplyIn>
-__device__ __forceinline__ void backward(int I, int O, int d, InPtr in_ptr, const float* out_rows,
-                                         int DP, const float2* corrP, float4 (&md)[OM][DCH],
-                                         ApplyIn apply_in) {
+__device__ __forceinline__ void backward(int I, int O, int d, InPtr in_ptr, const float* outI,
+                                         const float2* corrP, float4 (&md)[OM][DCH], ApplyIn apply_in) {
   typedef StepShape<OM> SS;
   const int lane = lane_id();
   const int d4 = d >> 2;
@@ -440,16 +457,18 @@ __device__ __forceinline__ void backward(int I, int O, int d, InPtr in_ptr, cons
   for (int i = 0; i < OM; i++)
 #pragma unroll
     for (int t = 0; t < DCH; t++) md[i][t] = make_float4(mlo[i][t].x, mlo[i][t].y, mhi[i][t].x, mhi[i][t].y);
-  float2 olo[OM][DCH], ohi[OM][DCH];
+  float2 olo[SS::OMP][DCH], ohi[SS::OMP][DCH];
 #pragma unroll
-  for (int i = 0; i < OM; i++)
+  for (int pp = 0; pp < SS::NPAIR; pp++)
 #pragma unroll
     for (int t = 0; t < DCH; t++) {
       const int q = lane + 32 * t;
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (i < O && q < d4) v = reinterpret_cast<const float4*>(out_rows + (size_t)i * DP)[q];
-      olo[i][t] = make_float2(v.x, v.y);
-      ohi[i][t] = make_float2(v.z, v.w);
+      float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0;
+      if (2 * pp < O && q < d4) out_chunk_pair(outI, d, pp, q, r0, r1);
+      olo[2 * pp][t] = make_float2(r0.x, r0.y);
+      ohi[2 * pp][t] = make_float2(r0.z, r0.w);
+      olo[2 * pp + 1][t] = make_float2(r1.x, r1.y);
+      ohi[2 * pp + 1][t] = make_float2(r1.z, r1.w);
     }
   // four inputs per iteration: eight independent chains; updates applied in input order
   for (int j0 = 0; j0 < I; j0 += 4) {
@@ -490,10 +509,9 @@ __device__ __forceinline__ void backward(int I, int O, int d, InPtr in_ptr, cons
   __syncwarp();
 }
 
-// Stores the step's output rows from registers in both layouts (see StepShape).
+// Stores the step's output rows from registers in the interleaved layout (see StepShape).
 template <int OM, int DCH>
-__device__ __forceinline__ void store_out_rows(const float4 (&v)[OM][DCH], int O, int d, float* out_rows,
-                                               int DP, float* outI) {
+__device__ __forceinline__ void store_out_interleaved(const float4 (&v)[OM][DCH], int O, int d, float* outI) {
   typedef StepShape<OM> SS;
   const int lane = lane_id(), d4 = d >> 2;
 #pragma unroll
@@ -501,13 +519,11 @@ __device__ __forceinline__ void store_out_rows(const float4 (&v)[OM][DCH], int O
     const int q = lane + 32 * t;
     if (q < d4) {
 #pragma unroll
-      for (int i = 0; i < OM; i++)
-        if (i < O) reinterpret_cast<float4*>(out_rows + (size_t)i * DP)[q] = v[i][t];
-#pragma unroll
       for (int p = 0; p < SS::NPAIR; p++) {
         if (2 * p < O) {
           const float4 a = v[2 * p][t];
-          const float4 b = (2 * p + 1 < O) ? v[2 * p + 1][t] : make_float4(0.f, 0.f, 0.f, 0.f);
+          const float4 b = (2 * p + 1 < OM && 2 * p + 1 < O) ? v[(2 * p + 1) < OM ? 2 * p + 1 : 0][t]
+                                                            : make_float4(0.f, 0.f, 0.f, 0.f);
           float4* dst = reinterpret_cast<float4*>(outI + ((size_t)p * d + 4 * q) * 2);
           dst[0] = make_float4(a.x, b.x, a.y, b.y);
           dst[1] = make_float4(a.z, b.z, a.w, b.w);

@@ -66,7 +66,8 @@ constexpr int kPlainWarps = 4;
 __host__ __device__ inline size_t plain_warp_words(int d, int w, int K) {
   (void)K;
   const int DP = d + 4;
-  return align_up((size_t)kOMax * DP + (size_t)kOMax * d + (size_t)4 * w * (kOMax + 2) * 2 + 4 * w + 3 * kOMax, 4);
+  (void)DP;
+  return align_up((size_t)kOMax * d + (size_t)4 * w * (kOMax + 2) * 2 + 4 * w + 3 * kOMax, 4);
 }
 
 template <int S>
@@ -135,10 +136,8 @@ __global__ void __launch_bounds__(32 * kPlainWarps) plain_step_kernel(TrainParam
   if (wid >= p.workers) return;
 
   const int d = p.d, w = p.window, K = p.K, lmax = p.lmax;
-  const int DP = d + 4;
   float* wsm = smem + 1136 + (size_t)(threadIdx.x >> 5) * plain_warp_words(d, w, K);
-  float* out_rows = wsm;
-  float* outI = out_rows + (size_t)kOMax * DP;
+  float* outI = wsm;
   float2* corrP = reinterpret_cast<float2*>(outI + (size_t)kOMax * d);
   int* in_off = reinterpret_cast<int*>(corrP + (size_t)4 * w * (kOMax + 2));
   int* out_id = in_off + 4 * w;
@@ -259,7 +258,7 @@ __global__ void __launch_bounds__(32 * kPlainWarps) plain_step_kernel(TrainParam
           }
           v[i][t] = x;
         }
-      store_out_rows<kOMax, DCH>(v, O, d, out_rows, DP, outI);
+      store_out_interleaved<kOMax, DCH>(v, O, d, outI);
     }
     __syncwarp();
     const float alpha = *reinterpret_cast<volatile float*>(&p.ctr->alpha);
@@ -267,7 +266,7 @@ __global__ void __launch_bounds__(32 * kPlainWarps) plain_step_kernel(TrainParam
     forward_gradient<kOMax>(I, I0, O, d, in_ptr, outI, out_meta, exp_s, alpha, corrP, p.compute_loss != 0,
                             loss);
     float4 md[kOMax][DCH];
-    backward<kOMax, DCH>(I, O, d, in_ptr, out_rows, DP, corrP, md, add_to_input(in_ptr));
+    backward<kOMax, DCH>(I, O, d, in_ptr, outI, corrP, md, add_to_input(in_ptr));
     {
       uint64_t e1 = 0, e2 = 0;
       if (S == STORE_BF16) {

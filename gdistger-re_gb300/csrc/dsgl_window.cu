@@ -42,8 +42,8 @@ __host__ __device__ inline WinLayout win_layout(int d, int w, int K, int lmax) {
   L.IM = 4 * w;
   L.lmax = lmax;
   int off = 0;
-  L.rows = off;
-  off += (2 * L.NS + L.OM) * L.DP;
+  L.rows = off;  // window rows of both walks
+  off += 2 * L.NS * L.DP;
   L.outI = off;  // interleaved output rows (forward operand)
   off += L.OP * d;
   L.corr = off;  // duplicated gradient pairs, stride OP + 2 pairs per input
@@ -134,7 +134,6 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
   const WinLayout L = win_layout(d, w, K, p.lmax);
   float* base = smem + kHdrWords + (threadIdx.x >> 5) * L.words;
   float* rows = base + L.rows;
-  float* out_rows = rows + (size_t)2 * L.NS * L.DP;
   float* outI = base + L.outI;
   float2* corrP = reinterpret_cast<float2*>(base + L.corr);
   int* sen = reinterpret_cast<int*>(base + L.sen);
@@ -164,6 +163,14 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
   for (int s = lane; s < 2 * NS; s += 32) ref[s] = 0;
   float loss = 0.f;
   unsigned long long n_pairs = 0, n_steps = 0, n_outs = 0, n_loads = 0, n_stores = 0;
+  // negatives of the next step, drawn one step ahead when the pool stays (pf_g >= 0)
+  NegDraw pf{};
+  int pf_g = -1;
+  uint64_t pf_gs = 0;
+  // rows entering the windows at the last transition: loaded then, stored to their slots
+  // just before the next forward
+  float4 ent[2][DCH];
+  int ent_row[2] = {-1, -1};
   __syncwarp();
 
   // Places position `position` of walk `walk` in the window: an existing slot of the same
@@ -267,6 +274,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
       last_wc = 0;
       cur = start;
       len[0] = len[1] = 0;
+      ent_row[0] = ent_row[1] = -1;
       for (int s = lane; s < 2 * NS; s += 32) ref[s] = 0;
       __syncwarp();
       continue;
@@ -277,6 +285,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
       rng = jump_any(rng, (uint64_t)neg_n * (uint64_t)K, p.jumps);
       change_neg = false;
       grp_g = -1;
+      pf_g = -1;
     }
 
     // ---- one step (dsgl.hpp:1089-1368) ----
@@ -289,17 +298,36 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
                                      [&](int c) { return NS + ring[R + c % R]; });
     neg_count++;
     const int g = neg_count % neg_n;
-    uint64_t gs;
-    if (g == 0) gs = pool_base;
-    else if (g == grp_g + 1) gs = jump_small(grp_state, K, *sj);
-    else gs = jump_any(pool_base, (uint64_t)g * (uint64_t)K, p.jumps);
+    NegDraw nd;
+    if (g == pf_g) {
+      nd = pf;
+      grp_state = pf_gs;
+    } else {
+      uint64_t gs;
+      if (g == 0) gs = pool_base;
+      else if (g == grp_g + 1) gs = jump_small(grp_state, K, *sj);
+      else gs = jump_any(pool_base, (uint64_t)g * (uint64_t)K, p.jumps);
+      grp_state = gs;
+      nd = neg_draw_issue(p, *sj, gs);
+    }
     grp_g = g;
-    grp_state = gs;
-    const int O = select_outputs(p, *sj, gs, t1, t2, out_id, out_meta);
+    const int O = select_outputs(p, nd, t1, t2, out_id, out_meta);
     {  // gather the output rows (targets and negatives) from Woh, all loads in flight at once
       float4 v[OM][DCH];
       load_out_rows<S, OM, DCH>(p.woh, out_id, O, d, v);
-      store_out_rows<OM, DCH>(v, O, d, out_rows, DP, outI);
+      store_out_interleaved<OM, DCH>(v, O, d, outI);
+    }
+#pragma unroll
+    for (int walk = 0; walk < 2; walk++) {
+      if (ent_row[walk] >= 0) {
+        float4* dst = reinterpret_cast<float4*>(rows + (size_t)ent_row[walk] * DP);
+#pragma unroll
+        for (int t = 0; t < DCH; t++) {
+          const int q = lane + 32 * t;
+          if (q < (d >> 2)) dst[q] = ent[walk][t];
+        }
+        ent_row[walk] = -1;
+      }
     }
     __syncwarp();
     const float alpha = *reinterpret_cast<volatile float*>(&p.ctr->alpha);
@@ -310,7 +338,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     else
       forward_gradient<OM>(I, I0, O, d, in_ptr, outI, out_meta, exp_s, alpha, corrP, p.compute_loss != 0, loss);
     float4 md[OM][DCH];
-    backward<OM, DCH>(I, O, d, in_ptr, out_rows, DP, corrP, md, add_to_input(in_ptr));
+    backward<OM, DCH>(I, O, d, in_ptr, outI, corrP, md, add_to_input(in_ptr));
     {  // Woh += outputMd: target 1, target 2, then each negative (aliases follow that order)
       uint64_t e1 = 0, e2 = 0, en = 0;
       if (S == STORE_BF16) {
@@ -324,20 +352,23 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
         const int q = lane + 32 * t;
         if (q < d4) {
           float4 mlast = md[0][t];
-          float4 blast = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
           for (int i = 1; i < OM; i++)
             if (i == O - 1) mlast = md[i][t];
-          const float4 b1 = reinterpret_cast<const float4*>(out_rows)[q];
-          const float4 n1 = RowIO<S>::store4(p.woh, t1, d, q, add4(b1, md[0][t]), e1);
-          blast = t2 == t1 ? n1 : reinterpret_cast<const float4*>(out_rows + (size_t)(O - 1) * DP)[q];
+          float4 r0, r1;
+          out_chunk_pair(outI, d, 0, q, r0, r1);
+          const float4 n1 = RowIO<S>::store4(p.woh, t1, d, q, add4(r0, md[0][t]), e1);
+          float4 last0, last1;
+          out_chunk_pair(outI, d, (O - 1) >> 1, q, last0, last1);
+          const float4 blast = t2 == t1 ? n1 : (((O - 1) & 1) ? last1 : last0);
           const float4 n2 = RowIO<S>::store4(p.woh, t2, d, q, add4(blast, mlast), e2);
 #pragma unroll
           for (int i = 1; i < OM - 1; i++) {
             if (i < O - 1) {
               const int row = out_id[i];
-              const float4 bi = row == t2 ? n2
-                                          : reinterpret_cast<const float4*>(out_rows + (size_t)i * DP)[q];
+              float4 c0, c1;
+              out_chunk_pair(outI, d, i >> 1, q, c0, c1);
+              const float4 bi = row == t2 ? n2 : ((i & 1) ? c1 : c0);
               RowIO<S>::store4(p.woh, row, d, q, add4(bi, md[i][t]), en);
             }
           }
@@ -354,10 +385,10 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     pos[1]++;
     {
       // The memory order of the oracle: walk 0 (enter, leave), then walk 1 (enter, leave).
-      // An entering row's load is issued into registers at its place in that order and
-      // written to its slot after all four operations, so the loads overlap.
-      float4 ent[2][DCH];
-      int ent_row[2] = {-1, -1};
+      // An entering row's load is issued at its place in that order; its value is stored
+      // to the slot just before the next forward, so the load overlaps the next step's
+      // set-up.  A later write-back of the same vertex in this transition (walk 0's leave
+      // or flush before walk 1's enter reads) is ordered after the load by program order.
       const int d4 = d >> 2;
       for (int walk = 0; walk < 2; walk++) {
         const uint64_t ev =
@@ -385,22 +416,22 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
           if (P - w - 1 >= 0) leave(walk, P - w - 1, ev);
         }
       }
-#pragma unroll
-      for (int walk = 0; walk < 2; walk++) {
-        if (ent_row[walk] >= 0) {
-          float4* dst = reinterpret_cast<float4*>(rows + (size_t)ent_row[walk] * DP);
-#pragma unroll
-          for (int t = 0; t < DCH; t++) {
-            const int q = lane + 32 * t;
-            if (q < d4) dst[q] = ent[walk][t];
-          }
-        }
-      }
-      __syncwarp();
     }
     if (train_sen_num >= 2) {
       change_neg = true;
       train_sen_num = 0;
+    }
+    if (!change_neg) {  // the pool stays: draw the next step's negatives now
+      const int gn = (neg_count + 1) % neg_n;
+      uint64_t gs;
+      if (gn == 0) gs = pool_base;
+      else if (gn == grp_g + 1) gs = jump_small(grp_state, K, *sj);
+      else gs = jump_any(pool_base, (uint64_t)gn * (uint64_t)K, p.jumps);
+      pf = neg_draw_issue(p, *sj, gs);
+      pf_gs = gs;
+      pf_g = gn;
+    } else {
+      pf_g = -1;
     }
     step_id++;
   }

@@ -343,7 +343,7 @@ sgns_status autotune(sgns_handle* h) {
   double best = -1.0;
   int best_wpc = 1, best_workers = 0;
   sgns_status st = SGNS_OK;
-  for (int wpc : {1, 2, 4, 8}) {
+  for (int wpc = 1; wpc <= 8; wpc++) {
     int workers = 0;
     st = persistent_shape(h, wpc, &workers);
     if (st) {
