@@ -15,7 +15,7 @@ OUT = os.path.join(HERE, "build")
 ROOT = os.path.dirname(HERE)
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["dsgl_window.cu", "dsgl_plain.cu", "dsgl_aux.cu", "dsgl_adjoint.cu"]
+CU_SOURCES = ["dsgl_window.cu", "dsgl_plain.cu", "dsgl_aux.cu", "dsgl_adjoint.cu", "dsgl_noalloc.cu"]
 CPP_SOURCES = ["sgns_host.cpp"]
 LIB = os.path.join(OUT, "libsgns.so")
 CLI = os.path.join(OUT, "sgns_train")
@@ -46,7 +46,7 @@ def build(verbose_ptxas=False, force=False):
         objs.append(o)
         if force or _stale(o, [s] + headers):
             cmd = [NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                                   "-c", s, "-o", o]
+                                   "-I", os.path.join(ROOT, "include"), "-c", s, "-o", o]
             if verbose_ptxas:
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append(cmd)

@@ -416,6 +416,20 @@ DeviceScratch* device_scratch() {
 
 }  // namespace
 
+namespace sgns {
+void host_exp_table(float* t) { build_exp_table(t); }
+int report_error(int status, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  std::lock_guard<std::mutex> g(g_create_err_mx);
+  g_create_err = buf;
+  return status;
+}
+}  // namespace sgns
+
 // ===================================================================================
 extern "C" {
 

@@ -184,6 +184,10 @@ cudaError_t launch_minibatch(int d, int n, int imax, int omax, const int32_t* in
                              const float* alpha, const float* in_rows, const float* out_rows, float* d_in,
                              float* d_out, const float* exp_table, int64_t* offsets, int32_t* status,
                              cudaStream_t s);
+// host helpers shared by the translation units (sgns_host.cpp)
+void host_exp_table(float* t /* kExpTableSize + 1 */);
+int report_error(int status, const char* fmt, ...);  // sets sgns_last_error(NULL); returns status
+
 size_t adjoint_scratch_bytes(int64_t V);
 cudaError_t launch_adjoint(int dtype, int d, int n, int64_t V, int64_t total_in, int64_t total_out,
                            const int32_t* in_ptr, const int32_t* in_ids, const int32_t* in_first,

@@ -88,6 +88,7 @@ def lib():
         L.sgns_device_tables.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp)]
         L.sgns_save_text.argtypes = [vp, ctypes.c_char_p]
         L.sgns_minibatch_update.argtypes = [i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+        L.sgns_minibatch_update_noalloc.argtypes = [i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
         L.sgns_loss_adjoint.argtypes = [i32, i32, i64, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp,
                                         ctypes.POINTER(i64), vp, vp, ctypes.POINTER(i64), vp]
         for name in header_functions():  # every declared entry point must be exported
@@ -221,6 +222,16 @@ def minibatch_update(d, in_count, in_first, out_count, out_meta, alpha, in_rows,
                                        out_meta.data_ptr(), alpha.data_ptr(), in_rows.data_ptr(),
                                        out_rows.data_ptr(), d_in.data_ptr(), d_out.data_ptr(),
                                        ctypes.c_void_p(stream)))
+
+
+def minibatch_update_noalloc(d, in_count, in_first, out_count, out_meta, alpha, in_rows, out_rows, d_in,
+                             d_out, stream=0):
+    """sgns_minibatch_update_noalloc: same arguments as minibatch_update, no device allocation."""
+    n = int(in_count.numel())
+    _check(lib().sgns_minibatch_update_noalloc(d, n, in_count.data_ptr(), in_first.data_ptr(), out_count.data_ptr(),
+                                               out_meta.data_ptr(), alpha.data_ptr(), in_rows.data_ptr(),
+                                               out_rows.data_ptr(), d_in.data_ptr(), d_out.data_ptr(),
+                                               ctypes.c_void_p(stream)))
 
 
 def loss_adjoint(dtype, d, V, in_ptr, in_ids, in_first, out_ptr, out_ids, out_meta, wih, woh, loss,

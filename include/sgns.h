@@ -149,6 +149,23 @@ sgns_status sgns_minibatch_update(int32_t d, int32_t n_batches, const int32_t* i
                                   const float* in_rows, const float* out_rows, float* d_in,
                                   float* d_out, void* stream);
 
+/* sgns_minibatch_update without any device allocation.  No counterpart in the
+ * reference: it exists for callers that cannot let a library allocate device memory --
+ * a process whose GPU memory belongs to its own allocator (a framework's caching
+ * allocator, a serving process that reserves the device up front), where cudaMalloc
+ * may fail, fragment the caller's pool, or synchronise the device mid-pipeline.
+ * Its scratch (row offsets, a status word, the sigmoid table) is a statically allocated
+ * device array of about 1 MiB that every GPU loading the library holds until exit;
+ * n is limited to 65536 minibatches (SGNS_EINVAL beyond).  The first call on a device
+ * resolves that array's address and fills the sigmoid table, so make it before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU (other
+ * streams, other threads) race on it.  Same arguments, results and limits otherwise. */
+sgns_status sgns_minibatch_update_noalloc(int32_t d, int32_t n_batches, const int32_t* in_count,
+                                          const int32_t* in_first, const int32_t* out_count,
+                                          const int32_t* out_meta, const float* alpha,
+                                          const float* in_rows, const float* out_rows, float* d_in,
+                                          float* d_out, void* stream);
+
 /* SGNS loss and its hand-written adjoint for n minibatches that index tables of V
  * rows (device pointers).  Minibatch b has inputs in_ids[in_ptr[b]..in_ptr[b+1]), the
  * first in_first[b] of them labelled by output 0 and the rest by the last output, and
