@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(32) minibatch_kernel(int d, int imax, int omax
   forward_gradient<kOMax>(I, first, O, d, in_ptr, outI, meta, exp_s, alpha[b], corrP, false, loss);
   float4 md[kOMax][DCH];
   float* gdin = d_in + in_off[b] * d;
-  backward<kOMax, DCH>(I, O, d, in_ptr, outI, corrP, md,
+  backward<kOMax, DCH>(I, O, d, in_ptr, [&](int pp, int q, float4& r0, float4& r1) { out_chunk_pair(outI, d, pp, q, r0, r1); }, corrP, md,
                        [&](int j, int q, float4 a) { reinterpret_cast<float4*>(gdin + (size_t)j * d)[q] = a; });
   float* gdout = d_out + out_off[b] * d;
 #pragma unroll

@@ -343,40 +343,42 @@ __device__ __forceinline__ void forward_gradient(int I, int first, int O, int d,
 }
 
 // Forward of the persistent engine: the same gradient, with each dot product summed as
-// four independent sequential quarter-sums over k combined as (s0 + s1) + (s2 + s3)
-// (d % 16 == 0).  Sixteen independent FFMA2 chains per lane instead of four 4x longer
-// ones; the oracle's window policy uses the same order.
+// eight independent sequential partial sums -- the even and the odd k of each quarter of
+// [0, d), each pair advanced by one FFMA2 on {o[k], o[k+1]} x {x[k], x[k+1]} -- combined
+// as s_m = even_m + odd_m, f = (s_0 + s_1) + (s_2 + s_3) when d % 16 == 0; when not,
+// [0, d) is one range and f = even + odd.  The oracle's window policy uses the same
+// order.  out_rows: normal layout, stride DP.
 template <int OM, class InPtr>
-__device__ __forceinline__ void forward_gradient_split4(int I, int first, int O, int d, InPtr in_ptr,
-                                                        const float* outI, const int* out_meta,
+__device__ __forceinline__ void forward_gradient_split8(int I, int first, int O, int d, InPtr in_ptr,
+                                                        const float* out_rows, int DP, const int* out_meta,
                                                         const float* exp_table, float alpha, float2* corrP,
                                                         bool want_loss, float& loss) {
   typedef StepShape<OM> SS;
   const int lane = lane_id();
-  const int q4 = d >> 4;  // chunks of 4 columns per quarter
+  const int nq = (d & 15) == 0 ? 4 : 1;  // quarters of [0, d) (one range when d % 16 != 0)
+  const int q4 = (d >> 2) / nq;          // chunks of 4 columns per quarter
   for (int j0 = 0; j0 < I; j0 += 32) {
     const int j = j0 + lane;
     const float4* x = reinterpret_cast<const float4*>(in_ptr(j < I ? j : I - 1));
-    float2 f[SS::NPAIR][4];
+    float2 f[OM][4];
 #pragma unroll
-    for (int q = 0; q < SS::NPAIR; q++)
+    for (int i = 0; i < OM; i++)
 #pragma unroll
-      for (int m = 0; m < 4; m++) f[q][m] = make_float2(0.f, 0.f);
+      for (int m = 0; m < 4; m++) f[i][m] = make_float2(0.f, 0.f);
     for (int k4 = 0; k4 < q4; k4++) {
       float4 xv[4];
 #pragma unroll
-      for (int m = 0; m < 4; m++) xv[m] = x[m * q4 + k4];
+      for (int m = 0; m < 4; m++) xv[m] = m < nq ? x[m * q4 + k4] : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-      for (int q = 0; q < SS::NPAIR; q++) {
-        if (2 * q < O) {
+      for (int i = 0; i < OM; i++) {
+        if (i < O) {
+          const float4* orow = reinterpret_cast<const float4*>(out_rows + (size_t)i * DP);
 #pragma unroll
           for (int m = 0; m < 4; m++) {
-            const float4* op = reinterpret_cast<const float4*>(outI + ((size_t)q * d + 4 * (m * q4 + k4)) * 2);
-            const float4 a = op[0], b = op[1];
-            f[q][m] = ffma2(make_float2(a.x, a.y), make_float2(xv[m].x, xv[m].x), f[q][m]);
-            f[q][m] = ffma2(make_float2(a.z, a.w), make_float2(xv[m].y, xv[m].y), f[q][m]);
-            f[q][m] = ffma2(make_float2(b.x, b.y), make_float2(xv[m].z, xv[m].z), f[q][m]);
-            f[q][m] = ffma2(make_float2(b.z, b.w), make_float2(xv[m].w, xv[m].w), f[q][m]);
+            if (m >= nq) continue;
+            const float4 o = orow[m * q4 + k4];
+            f[i][m] = ffma2(make_float2(o.x, o.y), make_float2(xv[m].x, xv[m].y), f[i][m]);
+            f[i][m] = ffma2(make_float2(o.z, o.w), make_float2(xv[m].z, xv[m].w), f[i][m]);
           }
         }
       }
@@ -386,8 +388,9 @@ __device__ __forceinline__ void forward_gradient_split4(int I, int first, int O,
       for (int i = 0; i < OM; i++) {
         if (i < O) {
           const int label = j < first ? (i == 0) : (i == O - 1);
-          const float2 s = fadd2(fadd2(f[i >> 1][0], f[i >> 1][1]), fadd2(f[i >> 1][2], f[i >> 1][3]));
-          const float fi = (i & 1) ? s.y : s.x;
+          const float s0 = __fadd_rn(f[i][0].x, f[i][0].y), s1 = __fadd_rn(f[i][1].x, f[i][1].y);
+          const float s2 = __fadd_rn(f[i][2].x, f[i][2].y), s3 = __fadd_rn(f[i][3].x, f[i][3].y);
+          const float fi = __fadd_rn(__fadd_rn(s0, s1), __fadd_rn(s2, s3));
           float g;
           if (fi > (float)kMaxExp) {
             g = __fmul_rn((float)(label - 1), alpha);
@@ -411,14 +414,31 @@ __device__ __forceinline__ void forward_gradient_split4(int I, int first, int O,
   __syncwarp();
 }
 
+// Stores the step's output rows from registers in the normal layout (stride DP).
+template <int OM, int DCH>
+__device__ __forceinline__ void store_out_normal(const float4 (&v)[OM][DCH], int O, int d, float* out_rows,
+                                                 int DP) {
+  const int lane = lane_id(), d4 = d >> 2;
+#pragma unroll
+  for (int t = 0; t < DCH; t++) {
+    const int q = lane + 32 * t;
+    if (q < d4) {
+#pragma unroll
+      for (int i = 0; i < OM; i++)
+        if (i < O) reinterpret_cast<float4*>(out_rows + (size_t)i * DP)[q] = v[i][t];
+    }
+  }
+}
+
 // Backward.  Lane owns column chunks q = lane + 32 t (t < DCH, q < d/4), as two pairs.
 //   md[i][t]  = sum_j corr[i][j] * in_j[q]     (outputMd, dsgl.hpp:1290), sequential j
 //   in_j[q]  += sum_i corr[i][j] * out_i[q]     (inputM then buffer +=, dsgl.hpp:1309-1333),
 //               sequential i, inputs applied in order j = 0..I-1.
 // md is complete before any input row changes, as the reference's two GEMMs read the
 // same pre-update inputM.  apply_in(j, q, a) consumes input j's update of chunk q.
-template <int OM, int DCH, class InPtr, class ApplyIn>
-__device__ __forceinline__ void backward(int I, int O, int d, InPtr in_ptr, const float* outI,
+// out_pair(p, q, r0, r1): rows 2p and 2p+1 of the step's outputs, columns 4q..4q+3.
+template <int OM, int DCH, class InPtr, class OutPair, class ApplyIn>
+__device__ __forceinline__ void backward(int I, int O, int d, InPtr in_ptr, OutPair out_pair,
                                          const float2* corrP, float4 (&md)[OM][DCH], ApplyIn apply_in) {
   typedef StepShape<OM> SS;
   const int lane = lane_id();
@@ -464,7 +484,7 @@ __device__ __forceinline__ void backward(int I, int O, int d, InPtr in_ptr, cons
     for (int t = 0; t < DCH; t++) {
       const int q = lane + 32 * t;
       float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0;
-      if (2 * pp < O && q < d4) out_chunk_pair(outI, d, pp, q, r0, r1);
+      if (2 * pp < O && q < d4) out_pair(pp, q, r0, r1);
       olo[2 * pp][t] = make_float2(r0.x, r0.y);
       ohi[2 * pp][t] = make_float2(r0.z, r0.w);
       olo[2 * pp + 1][t] = make_float2(r1.x, r1.y);

@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(32 * kPlainWarps) plain_step_kernel(TrainParam
     forward_gradient<kOMax>(I, I0, O, d, in_ptr, outI, out_meta, exp_s, alpha, corrP, p.compute_loss != 0,
                             loss);
     float4 md[kOMax][DCH];
-    backward<kOMax, DCH>(I, O, d, in_ptr, outI, corrP, md, add_to_input(in_ptr));
+    backward<kOMax, DCH>(I, O, d, in_ptr, [&](int pp, int q, float4& r0, float4& r1) { out_chunk_pair(outI, d, pp, q, r0, r1); }, corrP, md, add_to_input(in_ptr));
     {
       uint64_t e1 = 0, e2 = 0;
       if (S == STORE_BF16) {

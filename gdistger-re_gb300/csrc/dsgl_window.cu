@@ -12,8 +12,8 @@
 //   * the step's output rows (target of each walk + shared negatives) and gradients.
 // Negative rows are read from and added to Woh at each step, as the reference does for
 // the two target rows (dsgl.hpp:1346-1356).  Dot products of the forward are summed as
-// four sequential quarter-sums combined pairwise (when d % 16 == 0); the backward keeps
-// the reference's order.  The negative pool keeps the reference's
+// eight sequential partial sums (even and odd k of each quarter of [0, d)) combined
+// pairwise; the backward keeps the reference's order.  The negative pool keeps the reference's
 // draw stream (max(len1,len2)*K draws per pool, group neg_count % n per step,
 // dsgl.hpp:1054-1073, 1136-1154) but is regenerated from its base LCG state instead of
 // being stored.
@@ -44,8 +44,8 @@ __host__ __device__ inline WinLayout win_layout(int d, int w, int K, int lmax) {
   int off = 0;
   L.rows = off;  // window rows of both walks
   off += 2 * L.NS * L.DP;
-  L.outI = off;  // interleaved output rows (forward operand)
-  off += L.OP * d;
+  L.outI = off;  // the step's output rows, normal layout (stride DP)
+  off += L.OP * L.DP;
   L.corr = off;  // duplicated gradient pairs, stride OP + 2 pairs per input
   off += L.IM * (L.OP + 2) * 2;
   L.sen = off;
@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
   const WinLayout L = win_layout(d, w, K, p.lmax);
   float* base = smem + kHdrWords + (threadIdx.x >> 5) * L.words;
   float* rows = base + L.rows;
-  float* outI = base + L.outI;
+  float* out_rows = base + L.outI;
   float2* corrP = reinterpret_cast<float2*>(base + L.corr);
   int* sen = reinterpret_cast<int*>(base + L.sen);
   int* vert = reinterpret_cast<int*>(base + L.vert);
@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     {  // gather the output rows (targets and negatives) from Woh, all loads in flight at once
       float4 v[OM][DCH];
       load_out_rows<S, OM, DCH>(p.woh, out_id, O, d, v);
-      store_out_interleaved<OM, DCH>(v, O, d, outI);
+      store_out_normal<OM, DCH>(v, O, d, out_rows, DP);
     }
 #pragma unroll
     for (int walk = 0; walk < 2; walk++) {
@@ -332,13 +332,15 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     __syncwarp();
     const float alpha = *reinterpret_cast<volatile float*>(&p.ctr->alpha);
     auto in_ptr = [&](int j) -> const float* { return rows + (size_t)in_row[j] * DP; };
-    if ((d & 15) == 0)
-      forward_gradient_split4<OM>(I, I0, O, d, in_ptr, outI, out_meta, exp_s, alpha, corrP, p.compute_loss != 0,
-                                  loss);
-    else
-      forward_gradient<OM>(I, I0, O, d, in_ptr, outI, out_meta, exp_s, alpha, corrP, p.compute_loss != 0, loss);
+    forward_gradient_split8<OM>(I, I0, O, d, in_ptr, out_rows, DP, out_meta, exp_s, alpha, corrP,
+                                p.compute_loss != 0, loss);
     float4 md[OM][DCH];
-    backward<OM, DCH>(I, O, d, in_ptr, outI, corrP, md, add_to_input(in_ptr));
+    auto out_pair = [&](int pp, int q, float4& r0, float4& r1) {
+      r0 = reinterpret_cast<const float4*>(out_rows + (size_t)(2 * pp) * DP)[q];
+      r1 = 2 * pp + 1 < O ? reinterpret_cast<const float4*>(out_rows + (size_t)(2 * pp + 1) * DP)[q]
+                          : make_float4(0.f, 0.f, 0.f, 0.f);
+    };
+    backward<OM, DCH>(I, O, d, in_ptr, out_pair, corrP, md, add_to_input(in_ptr));
     {  // Woh += outputMd: target 1, target 2, then each negative (aliases follow that order)
       uint64_t e1 = 0, e2 = 0, en = 0;
       if (S == STORE_BF16) {
@@ -355,20 +357,16 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
 #pragma unroll
           for (int i = 1; i < OM; i++)
             if (i == O - 1) mlast = md[i][t];
-          float4 r0, r1;
-          out_chunk_pair(outI, d, 0, q, r0, r1);
-          const float4 n1 = RowIO<S>::store4(p.woh, t1, d, q, add4(r0, md[0][t]), e1);
-          float4 last0, last1;
-          out_chunk_pair(outI, d, (O - 1) >> 1, q, last0, last1);
-          const float4 blast = t2 == t1 ? n1 : (((O - 1) & 1) ? last1 : last0);
+          const float4 b1 = reinterpret_cast<const float4*>(out_rows)[q];
+          const float4 n1 = RowIO<S>::store4(p.woh, t1, d, q, add4(b1, md[0][t]), e1);
+          const float4 blast =
+              t2 == t1 ? n1 : reinterpret_cast<const float4*>(out_rows + (size_t)(O - 1) * DP)[q];
           const float4 n2 = RowIO<S>::store4(p.woh, t2, d, q, add4(blast, mlast), e2);
 #pragma unroll
           for (int i = 1; i < OM - 1; i++) {
             if (i < O - 1) {
               const int row = out_id[i];
-              float4 c0, c1;
-              out_chunk_pair(outI, d, i >> 1, q, c0, c1);
-              const float4 bi = row == t2 ? n2 : ((i & 1) ? c1 : c0);
+              const float4 bi = row == t2 ? n2 : reinterpret_cast<const float4*>(out_rows + (size_t)i * DP)[q];
               RowIO<S>::store4(p.woh, row, d, q, add4(bi, md[i][t]), en);
             }
           }

@@ -27,8 +27,8 @@
 //                    sliding window [pos-w, pos+w] (one copy per walk, exactly as the
 //                    reference dedupes them) and written back when they leave it;
 //                    negative rows are read from and added to Woh at each step; each
-//                    forward dot product is four sequential quarter-sums combined
-//                    pairwise (d % 16 == 0).
+//                    forward dot product is eight sequential partial sums (even and odd
+//                    k of each quarter of [0, d)) combined pairwise.
 // Storage: FP32, BF16 with stochastic rounding on every write-back, or FP64.
 #include <algorithm>
 #include <atomic>
@@ -462,23 +462,29 @@ struct Worker {
 
     // forward + gradient (dsgl.hpp:1241-1272, MKL branch labels)
     const A alpha = (A)sh.alpha.load(std::memory_order_relaxed);
-    // The window policy's engine sums each dot product as four sequential quarter-sums
-    // combined as (s0 + s1) + (s2 + s3) when d % 16 == 0; the reference order otherwise.
-    const bool split4 = sh.policy == POLICY_WINDOW && d % 16 == 0;
+    // The window policy's engine sums each dot product as eight sequential partial sums:
+    // the even and the odd k of each quarter of [0, d), s_m = even_m + odd_m, combined as
+    // (s0 + s1) + (s2 + s3); when d % 16 != 0, [0, d) is one range and f = even + odd.
+    const bool window_order = sh.policy == POLICY_WINDOW;
+    const int nq = d % 16 == 0 ? 4 : 1;
     for (int i = 0; i < O; i++) {
       const A c = (A)out_meta[i];
       for (int j = 0; j < I; j++) {
         A f = 0;
         const A* o = &outputM[(size_t)i * d];
         const A* x = &inputM[(size_t)j * d];
-        if (split4) {
-          const int qd = d / 4;
-          A s4[4];
-          for (int m = 0; m < 4; m++) {
-            s4[m] = 0;
-            for (int k = m * qd; k < (m + 1) * qd; k++) s4[m] = fma_acc(o[k], x[k], s4[m]);
+        if (window_order) {
+          const int qd = d / nq;
+          A s4[4] = {0, 0, 0, 0};
+          for (int m = 0; m < nq; m++) {
+            A ev = 0, od = 0;
+            for (int k = m * qd; k < (m + 1) * qd; k += 2) {
+              ev = fma_acc(o[k], x[k], ev);
+              od = fma_acc(o[k + 1], x[k + 1], od);
+            }
+            s4[m] = ev + od;
           }
-          f = (s4[0] + s4[1]) + (s4[2] + s4[3]);
+          f = nq == 4 ? (s4[0] + s4[1]) + (s4[2] + s4[3]) : s4[0];
         } else {
           for (int k = 0; k < d; k++) f = fma_acc(o[k], x[k], f);
         }
