@@ -216,6 +216,265 @@ def run_reference(args, wl):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------------
+# evaluation modes (not the headline line): link-prediction AUC across engines and the
+# CPU reference, bf16 per-minibatch error against fp64, the shape sweep, the adjoint.
+
+def _train_embedding(sgns, counts, corpus_np, V, engine, storage, device, **kw):
+    opt = sgns.default_options(iter=1, storage=storage, engine=engine, device=device, debug=0, **{**TRAIN, **kw})
+    with sgns.Trainer(opt) as t:
+        t.set_vocab(counts)
+        t.upload(corpus_np)
+        st = t.train()
+        emb = np.zeros((V, opt.size), np.float32)
+        emb[t.order()] = t.embeddings(0)
+        return emb, st
+
+
+def run_auc(args):
+    """SBM graph with a 10% holdout, information-oriented walks (lengths 21-80, mean ~40);
+    the same corpus trained by every engine and by the CPU reference restatement."""
+    import torch
+    import sgns
+    import synth
+    import oracle
+
+    V, E = args.auc_vertices, int(args.auc_vertices * 2.73)
+    dev = "cuda"
+    ip, ix, _ = synth.sbm(V, E, blocks=4, ratio=20.0, seed=31, device=dev)
+    tr_ip, tr_ix, pos, neg = synth.holdout(ip, ix, 0.1, seed=32)
+    corpus = synth.information_walks(tr_ip, tr_ix, 10, 20, 80, 0.84, seed=33)
+    c = corpus.cpu().numpy().astype(np.int32)
+    counts = np.bincount(c[c >= 0], minlength=V).astype(np.int32)
+    ends = np.flatnonzero(c == -1)
+    lens = np.diff(np.concatenate([[-1], ends])) - 1
+    out = {"mode": "auc", "graph": "SBM V=%d E=%d 4 blocks p_in/p_out=20, 10%% holdout" % (V, ix.numel() // 2),
+           "walks": "10/vertex information-oriented, length mean %.1f (min %d, max %d)" % (lens.mean(), lens.min(), lens.max()),
+           "tokens": int(len(c)), "train": {**TRAIN, "iter": 1}}
+    for name, eng, sto in (("gpu_plain_fp32", "plain", "fp32"), ("gpu_persistent_fp32", "persistent", "fp32"),
+                           ("gpu_persistent_bf16", "persistent", "bf16")):
+        emb, st = _train_embedding(sgns, counts, c, V, eng, sto, 0)
+        out[name] = {"auc": synth.link_auc(emb, pos, neg), "pairs_per_s": st.pairs / st.train_ms * 1e3,
+                     "workers": st.workers}
+    if not args.auc_skip_cpu:
+        cores = os.cpu_count() or 1
+        t0 = time.time()
+        wih, _, st = oracle.train(c, counts, d=TRAIN["size"], window=TRAIN["window"], negative=TRAIN["negative"],
+                                  iter=1, workers=cores, threads=cores, table_threads=TRAIN["threads"],
+                                  policy=oracle.POLICY_REF, storage=oracle.STORE_F32, table_size=TRAIN["table_size"],
+                                  sample=TRAIN["sample"], alpha=TRAIN["alpha"])
+        order, _, _, _ = oracle.vocab(counts)
+        emb = np.zeros((V, TRAIN["size"]), np.float32)
+        emb[order] = wih
+        out["cpu_reference_fp32"] = {"auc": synth.link_auc(emb, pos, neg),
+                                     "pairs_per_s": st["pairs"] / (time.time() - t0), "threads": cores,
+                                     "kind": "oracle restatement of include/dsgl.hpp, reference buffer policy"}
+    b = out["gpu_persistent_bf16"]["auc"]
+    out["bf16_minus_fp32_auc"] = b - out["gpu_persistent_fp32"]["auc"]
+    if "cpu_reference_fp32" in out:
+        out["gpu_plain_fp32_minus_cpu_auc"] = out["gpu_plain_fp32"]["auc"] - out["cpu_reference_fp32"]["auc"]
+        out["gpu_persistent_bf16_minus_cpu_auc"] = b - out["cpu_reference_fp32"]["auc"]
+    print(json.dumps(out), flush=True)
+
+
+def reference_minibatches(corpus, V, n, w, K, seed, device):
+    """n minibatches shaped like reference steps (dsgl.hpp:1089-1159): a target and its
+    window from each of two walks, K shared negatives (uniform ids here), multiplicities."""
+    import torch
+
+    g = torch.Generator(device=device).manual_seed(seed)
+    c = corpus.to(device)
+    ends = torch.nonzero(c == -1).flatten()
+    starts = torch.cat([torch.zeros(1, dtype=torch.long, device=device), ends[:-1] + 1])
+    lens = ends - starts
+    ok = torch.nonzero(lens >= 2).flatten()
+    in_ids, in_ptr, first, out_ids, out_ptr, meta = [], [0], [], [], [0], []
+    walks = ok[torch.randint(0, ok.numel(), (2 * n,), generator=g, device=device)].cpu().numpy()
+    st_np, ln_np = starts.cpu().numpy(), lens.cpu().numpy()
+    cc = c.cpu().numpy()
+    rng = np.random.default_rng(seed)
+    for b in range(n):
+        ctx, tg = [], []
+        bb = int(rng.integers(0, w))
+        for wk in walks[2 * b: 2 * b + 2]:
+            s0, L = st_np[wk], ln_np[wk]
+            pos = int(rng.integers(0, L))
+            tg.append(int(cc[s0 + pos]))
+            ctx.append([int(cc[s0 + pos - w + i]) for i in range(bb, 2 * w + 1 - bb)
+                        if i != w and 0 <= pos - w + i < L])
+        negs = rng.integers(1, V, K)
+        outs, mt = [tg[0]], [1]
+        for s_ in negs:
+            s_ = int(s_)
+            if s_ in outs:
+                k = outs.index(s_)
+                if k > 0:
+                    mt[k] += 1
+            else:
+                outs.append(s_)
+                mt.append(1)
+        outs.append(tg[1])
+        mt.append(1)
+        in_ids += ctx[0] + ctx[1]
+        in_ptr.append(len(in_ids))
+        first.append(len(ctx[0]))
+        out_ids += outs
+        out_ptr.append(len(out_ids))
+        meta += mt
+    return in_ids, in_ptr, first, out_ids, out_ptr, meta
+
+
+def run_minibatch_error(args):
+    """bf16 form, per minibatch: the fp32 update (the trainers' arithmetic) and the
+    stochastically rounded bf16 rows it stores, against an fp64 oracle, on 1000
+    reference-shaped minibatches over the rows of a bf16 training run."""
+    import torch
+    import sgns
+    import synth
+    import oracle
+
+    wl = WORKLOADS["small"]
+    dev = "cuda"
+    ip, ix = synth.chung_lu(wl["V"], wl["E"], wl["gamma"], seed=2024, device=dev)
+    L = synth.walk_lengths(wl["V"] * 2, "geometric", mean=40, cap=80, seed=5, device=dev)
+    corpus = synth.random_walks(ip, ix, 2, L, seed=6)
+    c = corpus.cpu().numpy().astype(np.int32)
+    counts = np.bincount(c[c >= 0], minlength=wl["V"]).astype(np.int32)
+    opt = sgns.default_options(iter=1, storage="bf16", engine="persistent", device=0, debug=0, **TRAIN)
+    with sgns.Trainer(opt) as t:
+        t.set_vocab(counts)
+        t.upload(c)
+        t.train()
+        wih, woh = t.embeddings(0), t.embeddings(1)  # bf16 values, sorted-row order
+        row_of = np.empty(wl["V"], np.int64)
+        row_of[t.order()] = np.arange(wl["V"])
+    ii, ip_, ff, oo, op_, mm = reference_minibatches(corpus, wl["V"], 1000, TRAIN["window"], TRAIN["negative"], 7, dev)
+    xin = wih[row_of[np.asarray(ii)]]
+    xout = woh[row_of[np.asarray(oo)]]
+    tt = lambda a, dt=torch.int32: torch.tensor(np.asarray(a), dtype=dt, device=dev)
+    in_count = tt(np.diff(ip_))
+    out_count = tt(np.diff(op_))
+    alpha = torch.full((1000,), TRAIN["alpha"], dtype=torch.float32, device=dev)
+    d_in = torch.empty((len(ii), TRAIN["size"]), device=dev)
+    d_out = torch.empty((len(oo), TRAIN["size"]), device=dev)
+    sgns.minibatch_update(TRAIN["size"], in_count, tt(ff), out_count, tt(mm), alpha, torch.tensor(xin, device=dev),
+                          torch.tensor(xout, device=dev), d_in, d_out)
+    gi, go = d_in.cpu().numpy().astype(np.float64), d_out.cpu().numpy().astype(np.float64)
+    rng = np.random.default_rng(9)
+
+    def sr_bf16(x):  # the rounding rule of the kernels: add 16 uniform bits, truncate
+        u = x.astype(np.float32).view(np.uint32).astype(np.uint64)
+        r = rng.integers(0, 1 << 16, size=u.shape, dtype=np.uint64)
+        return (((u + r) >> 16).astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+
+    upd_err, row_err = [], []
+    oi = oo_ = 0
+    for b in range(1000):
+        I, O = ip_[b + 1] - ip_[b], op_[b + 1] - op_[b]
+        x0, o0 = xin[oi:oi + I].astype(np.float64), xout[oo_:oo_ + O].astype(np.float64)
+        dIn, dOut = oracle.minibatch(x0, o0, mm[op_[b]:op_[b + 1]], ff[b], TRAIN["alpha"], acc64=True)
+        for got, ref, base in ((gi[oi:oi + I], dIn, x0), (go[oo_:oo_ + O], dOut, o0)):
+            nref = np.linalg.norm(ref)
+            if nref > 0:
+                upd_err.append(np.linalg.norm(got - ref) / nref)
+            new64 = base + ref
+            new_bf16 = sr_bf16(base + got)
+            row_err.append(np.max(np.linalg.norm(new_bf16 - new64, axis=1) / np.maximum(np.linalg.norm(new64, axis=1), 1e-30)))
+        oi += I
+        oo_ += O
+    q = lambda a: {"median": float(np.median(a)), "p99": float(np.quantile(a, 0.99)), "max": float(np.max(a))}
+    print(json.dumps({"mode": "minibatch-error", "minibatches": 1000, "d": TRAIN["size"],
+                      "fp32_update_rel_err_vs_fp64": q(upd_err), "bf16_stored_row_rel_err_vs_fp64": q(row_err)}),
+          flush=True)
+
+
+def run_sweep(args):
+    """Walk lengths uniform in 5-200 on the LJ-sized Chung-Lu graph; d x K x storage:
+    the persistent engine (autotuned shape) against the plain engine (1/16 slice)."""
+    import torch
+    import sgns
+    import synth
+
+    wl = WORKLOADS["lj-cl"]
+    dev = "cuda"
+    ip, ix = synth.chung_lu(wl["V"], wl["E"], wl["gamma"], seed=2024, device=dev)
+    L = synth.walk_lengths(wl["V"], "uniform", lo=5, hi=200, seed=11, device=dev)
+    corpus = synth.random_walks(ip, ix, 1, L, seed=12)
+    c = corpus.cpu().numpy().astype(np.int32)
+    counts = np.bincount(c[c >= 0], minlength=wl["V"]).astype(np.int32)
+    ends = np.flatnonzero(c == -1)
+    cut = int(ends[len(ends) // 16]) + 1
+    rows = []
+    for d in (64, 128, 256):
+        for K in (5, 10):
+            for sto in ("bf16", "fp32"):
+                kw = dict(TRAIN, size=d, negative=K)
+                o = sgns.default_options(iter=1, storage=sto, engine="persistent", device=0, debug=0, **kw)
+                with sgns.Trainer(o) as t:
+                    t.set_vocab(counts)
+                    t.upload(c)
+                    t.train()
+                    st = t.train()
+                po = sgns.default_options(iter=1, storage=sto, engine="plain", device=0, debug=0, **kw)
+                with sgns.Trainer(po) as t:
+                    t.set_vocab(counts)
+                    t.upload(c[:cut])
+                    ps = t.train()
+                rows.append({"d": d, "K": K, "storage": sto, "persistent_pairs_per_s": st.pairs / st.train_ms * 1e3,
+                             "warps_per_cta": st.warps_per_cta, "workers": st.workers,
+                             "plain_pairs_per_s": ps.pairs / ps.train_ms * 1e3,
+                             "speedup": (st.pairs / st.train_ms) / (ps.pairs / ps.train_ms)})
+                print(json.dumps(rows[-1]), flush=True)
+    print(json.dumps({"mode": "sweep", "graph": "Chung-Lu V=%d E=%d" % (wl["V"], ix.numel() // 2),
+                      "walks": "1/vertex, uniform lengths 5-200", "tokens": int(len(c)), "rows": rows}), flush=True)
+
+
+def run_adjoint(args):
+    """Forward + hand-written adjoint on reference-shaped minibatches over a 4M-vertex
+    Chung-Lu graph, bf16 tables with fp32 accumulation; row-gradient GB/s."""
+    import torch
+    import sgns
+    import synth
+
+    V = args.adj_vertices
+    dev = "cuda"
+    ip, ix = synth.chung_lu(V, 15 * V, 2.1, seed=41, device=dev)
+    L = synth.walk_lengths(200000, "geometric", mean=40, cap=80, seed=42, device=dev)
+    # walks from a random sample of start vertices are enough to shape the minibatches
+    corpus = synth.random_walks(ip, ix, 1, 40, seed=43)[: 40 * 200000]
+    nb = args.adj_batches
+    ii, ip_, ff, oo, op_, mm = reference_minibatches(corpus, V, nb, TRAIN["window"], TRAIN["negative"], 44, dev)
+    tt = lambda a: torch.tensor(np.asarray(a), dtype=torch.int32, device=dev)
+    in_ids, in_ptr, first, out_ids, out_ptr, meta = tt(ii), tt(ip_), tt(ff), tt(oo), tt(op_), tt(mm)
+    d = TRAIN["size"]
+    g = torch.Generator(device=dev).manual_seed(1)
+    wih = ((torch.rand((V, d), generator=g, device=dev) - 0.5) / d).to(torch.bfloat16)
+    woh = ((torch.rand((V, d), generator=g, device=dev) - 0.5) / d).to(torch.bfloat16)
+    loss = torch.zeros(1, dtype=torch.float64, device=dev)
+    gi_ids = torch.empty(len(ii), dtype=torch.int32, device=dev)
+    go_ids = torch.empty(len(oo), dtype=torch.int32, device=dev)
+    gi = torch.empty((len(ii), d), device=dev)
+    go = torch.empty((len(oo), d), device=dev)
+    stream = torch.cuda.current_stream().cuda_stream
+    call = lambda: sgns.loss_adjoint(1, d, V, in_ptr, in_ids, first, out_ptr, out_ids, meta, wih.data_ptr(),
+                                     woh.data_ptr(), loss, gi_ids, gi, go_ids, go, stream=stream)
+    for _ in range(2):
+        call()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reps = 5
+    for _ in range(reps):
+        n_in, n_out = call()
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / reps
+    grad_bytes = (n_in + n_out) * (d * 4 + 4)
+    print(json.dumps({"mode": "adjoint", "graph": "Chung-Lu V=%d E=%d" % (V, ix.numel() // 2), "d": d,
+                      "minibatches": nb, "inputs": len(ii), "outputs": len(oo), "unique_in_rows": n_in,
+                      "unique_out_rows": n_out, "ms_per_call": dt * 1e3,
+                      "row_gradient_GBps": grad_bytes / dt / 1e9, "loss": float(loss.item()),
+                      "storage": "bf16 tables, fp32 accumulation"}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -225,10 +484,25 @@ def main():
     ap.add_argument("--workload", default="lj-cl", choices=sorted(WORKLOADS))
     ap.add_argument("--skip-extras", action="store_true", help="only the timed bf16 steps (profiling runs)")
     ap.add_argument("--wpc", type=int, default=0, help="warps per CTA of the persistent engine (0 = autotune)")
+    ap.add_argument("--auc", action="store_true", help="link-prediction AUC of every engine and the CPU reference")
+    ap.add_argument("--auc-vertices", type=int, default=100000)
+    ap.add_argument("--auc-skip-cpu", action="store_true")
+    ap.add_argument("--mb-error", action="store_true", help="bf16 per-minibatch error against fp64")
+    ap.add_argument("--sweep", action="store_true", help="d x K x storage sweep, persistent vs plain")
+    ap.add_argument("--adjoint", action="store_true", help="loss + adjoint throughput (row-gradient GB/s)")
+    ap.add_argument("--adj-vertices", type=int, default=4_000_000)
+    ap.add_argument("--adj-batches", type=int, default=200_000)
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
         return run_reference(args, wl)
+    for flag, fn in (("auc", run_auc), ("mb_error", run_minibatch_error), ("sweep", run_sweep),
+                     ("adjoint", run_adjoint)):
+        if getattr(args, flag):
+            import torch
+
+            torch.cuda.set_device(0)
+            return fn(args)
 
     import torch
 
