@@ -29,12 +29,27 @@ __device__ __forceinline__ int nth_set_bit(unsigned x, int n) {
   return __ffs(x) - 1;
 }
 
+// Stochastic rounding of two floats to a bf16 pair in one instruction (sm_100a and later):
+// lo gets rbits[15:0] and lands in the low half, hi gets rbits[31:16].  For every non-NaN
+// input the result equals truncating (bits(x) + r16) to its upper 16 bits; NaN becomes
+// 0x7FFF.
+__device__ __forceinline__ uint32_t cvt_rs_bf16x2(float lo, float hi, uint32_t rbits) {
+  uint32_t d;
+  asm("cvt.rs.bf16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(rbits));
+  return d;
+}
+
 // ---- storage rows ------------------------------------------------------------------
 // A row of d elements; column chunk q holds columns 4q..4q+3 (d % 4 == 0).
 template <int S> struct RowIO;
 
 template <> struct RowIO<STORE_F32> {
   static constexpr int kBytes = 4;
+  typedef float4 Raw;  // a chunk as loaded, before widening to fp32
+  __device__ static __forceinline__ Raw load_raw(const void* base, int64_t row, int d, int q) {
+    return reinterpret_cast<const float4*>(static_cast<const float*>(base) + row * d)[q];
+  }
+  __device__ static __forceinline__ float4 widen(Raw r) { return r; }
   __device__ static __forceinline__ float4 load4(const void* base, int64_t row, int d, int q) {
     return reinterpret_cast<const float4*>(static_cast<const float*>(base) + row * d)[q];
   }
@@ -47,23 +62,27 @@ template <> struct RowIO<STORE_F32> {
 
 template <> struct RowIO<STORE_BF16> {
   static constexpr int kBytes = 2;
-  __device__ static __forceinline__ float4 load4(const void* base, int64_t row, int d, int q) {
-    uint2 u = reinterpret_cast<const uint2*>(static_cast<const uint16_t*>(base) + row * d)[q];
+  typedef uint2 Raw;
+  __device__ static __forceinline__ Raw load_raw(const void* base, int64_t row, int d, int q) {
+    return reinterpret_cast<const uint2*>(static_cast<const uint16_t*>(base) + row * d)[q];
+  }
+  __device__ static __forceinline__ float4 widen(Raw u) {
     return make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xFFFF0000u),
                        __uint_as_float(u.y << 16), __uint_as_float(u.y & 0xFFFF0000u));
   }
+  __device__ static __forceinline__ float4 load4(const void* base, int64_t row, int d, int q) {
+    return widen(load_raw(base, row, d, q));
+  }
   // Stores with stochastic rounding; returns the values actually stored (as fp32).
+  // Column 4q+j takes random bits [16j, 16j+16) of sr_bits4.
   __device__ static __forceinline__ float4 store4(void* base, int64_t row, int d, int q, float4 v,
                                                   uint64_t ev) {
-    uint64_t bits = sr_bits4(ev, (uint32_t)row, (uint32_t)q);
-    uint32_t h0 = bf16_sr(v.x, (uint32_t)(bits)&0xFFFF);
-    uint32_t h1 = bf16_sr(v.y, (uint32_t)(bits >> 16) & 0xFFFF);
-    uint32_t h2 = bf16_sr(v.z, (uint32_t)(bits >> 32) & 0xFFFF);
-    uint32_t h3 = bf16_sr(v.w, (uint32_t)(bits >> 48) & 0xFFFF);
-    uint2 u = make_uint2(h0 | (h1 << 16), h2 | (h3 << 16));
+    const uint64_t bits = sr_bits4(ev, (uint32_t)row, (uint32_t)q);
+    const uint2 u = make_uint2(cvt_rs_bf16x2(v.x, v.y, (uint32_t)bits),
+                               cvt_rs_bf16x2(v.z, v.w, (uint32_t)(bits >> 32)));
     reinterpret_cast<uint2*>(static_cast<uint16_t*>(base) + row * d)[q] = u;
-    return make_float4(__uint_as_float(h0 << 16), __uint_as_float(h1 << 16),
-                       __uint_as_float(h2 << 16), __uint_as_float(h3 << 16));
+    return make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xFFFF0000u),
+                       __uint_as_float(u.y << 16), __uint_as_float(u.y & 0xFFFF0000u));
   }
 };
 

@@ -167,9 +167,9 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
   NegDraw pf{};
   int pf_g = -1;
   uint64_t pf_gs = 0;
-  // rows entering the windows at the last transition: loaded then, stored to their slots
-  // just before the next forward
-  float4 ent[2][DCH];
+  // rows entering the windows at the last transition: loaded then, widened and stored to
+  // their slots just before the next forward (so no instruction waits on the load earlier)
+  typename RowIO<S>::Raw ent[2][DCH];
   int ent_row[2] = {-1, -1};
   __syncwarp();
 
@@ -289,6 +289,10 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     }
 
     // ---- one step (dsgl.hpp:1089-1368) ----
+    // The step's stochastic-rounding event keys, computed off the write-back paths: lane k
+    // holds the key of event kind k (targets 1 and 2, walks 0 and 1, negatives).
+    const uint64_t sr_key =
+        S == STORE_BF16 && lane <= EV_NEG ? sr_event_key(p.sr_seed, lane, (uint32_t)wid, step_id) : 0;
     const int t1 = sen[pos[0]], t2 = sen[lmax + pos[1]];
     rng = lcg_next(rng);
     const int b = (int)fast_mod(rng, p.div_window);
@@ -324,7 +328,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
 #pragma unroll
         for (int t = 0; t < DCH; t++) {
           const int q = lane + 32 * t;
-          if (q < (d >> 2)) dst[q] = ent[walk][t];
+          if (q < (d >> 2)) dst[q] = RowIO<S>::widen(ent[walk][t]);
         }
         ent_row[walk] = -1;
       }
@@ -344,9 +348,9 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     {  // Woh += outputMd: target 1, target 2, then each negative (aliases follow that order)
       uint64_t e1 = 0, e2 = 0, en = 0;
       if (S == STORE_BF16) {
-        e1 = sr_event_key(p.sr_seed, EV_TARGET1, (uint32_t)wid, step_id);
-        e2 = sr_event_key(p.sr_seed, EV_TARGET2, (uint32_t)wid, step_id);
-        en = sr_event_key(p.sr_seed, EV_NEG, (uint32_t)wid, step_id);
+        e1 = __shfl_sync(kFull, sr_key, EV_TARGET1);
+        e2 = __shfl_sync(kFull, sr_key, EV_TARGET2);
+        en = __shfl_sync(kFull, sr_key, EV_NEG);
       }
       const int d4 = d >> 2;
 #pragma unroll
@@ -389,8 +393,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
       // or flush before walk 1's enter reads) is ordered after the load by program order.
       const int d4 = d >> 2;
       for (int walk = 0; walk < 2; walk++) {
-        const uint64_t ev =
-            S == STORE_BF16 ? sr_event_key(p.sr_seed, EV_WALK0 + walk, (uint32_t)wid, step_id) : 0;
+        const uint64_t ev = S == STORE_BF16 ? __shfl_sync(kFull, sr_key, EV_WALK0 + walk) : 0;
         if (pos[walk] >= len[walk]) {
           flush_walk(walk, ev);
           len[walk] = 0;
@@ -405,7 +408,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
 #pragma unroll
               for (int t = 0; t < DCH; t++) {
                 const int q = lane + 32 * t;
-                if (q < d4) ent[walk][t] = RowIO<S>::load4(p.wih, v, d, q);
+                if (q < d4) ent[walk][t] = RowIO<S>::load_raw(p.wih, v, d, q);
               }
               ent_row[walk] = walk * NS + s;
               n_loads++;

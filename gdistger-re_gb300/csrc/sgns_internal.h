@@ -107,16 +107,6 @@ SGNS_HD uint64_t sr_event_key(uint64_t seed, int kind, uint32_t worker, uint64_t
 SGNS_HD uint64_t sr_bits4(uint64_t ev, uint32_t row, uint32_t col4) {
   return mix64(ev ^ ((uint64_t)row << 8) ^ (uint64_t)col4);
 }
-SGNS_HD uint16_t bf16_sr(float x, uint32_t r16) {
-  uint32_t u;
-#if defined(__CUDA_ARCH__)
-  u = __float_as_uint(x);
-#else
-  __builtin_memcpy(&u, &x, 4);
-#endif
-  if ((u & 0x7F800000u) == 0x7F800000u) return (uint16_t)((u >> 16) | ((u & 0xFFFF) ? 0x40u : 0u));
-  return (uint16_t)((u + r16) >> 16);
-}
 SGNS_HD float bf16_bits_to_f32(uint16_t b) {
   uint32_t u = (uint32_t)b << 16;
 #if defined(__CUDA_ARCH__)

@@ -74,11 +74,13 @@ inline float bf16_to_f32(uint16_t b) {
   std::memcpy(&f, &u, 4);
   return f;
 }
-// Stochastic rounding to bfloat16: add 16 uniform bits below the kept mantissa, truncate.
+// Stochastic rounding to bfloat16: add 16 uniform bits below the kept mantissa, truncate
+// (infinities stay infinite, finite values near the top may round up to infinity); NaN
+// becomes the canonical 0x7FFF, as the GPU's stochastic-rounding conversion does.
 inline uint16_t f32_to_bf16_sr(float x, uint32_t r16) {
   uint32_t u;
   std::memcpy(&u, &x, 4);
-  if ((u & 0x7F800000u) == 0x7F800000u) return (uint16_t)((u >> 16) | ((u & 0xFFFF) ? 0x40u : 0u));
+  if ((u & 0x7FFFFFFFu) > 0x7F800000u) return 0x7FFFu;
   return (uint16_t)((u + r16) >> 16);
 }
 
