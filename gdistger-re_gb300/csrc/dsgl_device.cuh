@@ -388,17 +388,17 @@ __device__ __forceinline__ void forward_gradient_split8(int I, int first, int O,
       float4 xv[4];
 #pragma unroll
       for (int m = 0; m < 4; m++) xv[m] = m < nq ? x[m * q4 + k4] : make_float4(0.f, 0.f, 0.f, 0.f);
+      // Rows i >= O hold stale but readable data; their sums are never used, so the loop
+      // runs over all OM rows without a branch.
 #pragma unroll
       for (int i = 0; i < OM; i++) {
-        if (i < O) {
-          const float4* orow = reinterpret_cast<const float4*>(out_rows + (size_t)i * DP);
+        const float4* orow = reinterpret_cast<const float4*>(out_rows + (size_t)i * DP);
 #pragma unroll
-          for (int m = 0; m < 4; m++) {
-            if (m >= nq) continue;
-            const float4 o = orow[m * q4 + k4];
-            f[i][m] = ffma2(make_float2(o.x, o.y), make_float2(xv[m].x, xv[m].y), f[i][m]);
-            f[i][m] = ffma2(make_float2(o.z, o.w), make_float2(xv[m].z, xv[m].w), f[i][m]);
-          }
+        for (int m = 0; m < 4; m++) {
+          if (m >= nq) continue;
+          const float4 o = orow[m * q4 + k4];
+          f[i][m] = ffma2(make_float2(o.x, o.y), make_float2(xv[m].x, xv[m].y), f[i][m]);
+          f[i][m] = ffma2(make_float2(o.z, o.w), make_float2(xv[m].z, xv[m].w), f[i][m]);
         }
       }
     }
