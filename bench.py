@@ -36,6 +36,12 @@ for _p in (os.path.join(ROOT, "gdistger-re_gb300"), os.path.join(ROOT, "oracle")
 
 METRIC = "SGNS pairs/sec on 1 GB300 (BF16 batched vs plain FP32, same AUC) + HBM roofline %"
 
+# DRAM bytes (read + write) per pair of the persistent BF16 kernel, from one-pass ncu
+# captures (dram__bytes_read.sum + dram__bytes_write.sum) of a whole training launch of
+# each workload at 7 warps/CTA; profiles/window_engine_lj-cl_dram.md gives the command.
+# The small workload's tables fit in L2, so its figure does not scale to the large one.
+NCU_DRAM_BYTES_PER_PAIR = {"lj-cl": 1429.11e9 / 7597249326, "small": 50.27e9 / 675874507}
+
 WORKLOADS = {
     "lj-cl": dict(V=2238731, E=30_000_000, gamma=2.1, walks=10, mean=40, cap=80),
     "small": dict(V=200_000, E=2_000_000, gamma=2.1, walks=10, mean=40, cap=80),
@@ -565,7 +571,10 @@ def main():
     peak = pk["hbm_gbs"] if pk else 6800.0
     table_traffic = (st_last.row_loads + st_last.row_stores + 2 * st_last.output_rows) * TRAIN["size"] * 2
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "peak_source": "measured" if pk else "fallback",
+                "traffic": (NCU_DRAM_BYTES_PER_PAIR[args.workload] * pairs / args.steps
+                            if args.workload in NCU_DRAM_BYTES_PER_PAIR else None),
+                "traffic_source": "ncu DRAM bytes per pair of this workload x pairs per launch",
+                "peak_source": "measured" if pk else "fallback",
                 "algorithmic_bytes_per_launch": bytes_per_launch,
                 "table_bytes_per_launch": float(table_traffic + 4 * n_tok),
                 "kernel_ms": float(np.mean(kernel_ms))}
