@@ -201,7 +201,10 @@ __device__ __forceinline__ NegDraw neg_draw_issue(const TrainParams& p, const Sm
   return n;
 }
 // Equal draws merge (meta = multiplicity, first occurrence keeps its place); draws equal
-// to t1 are dropped.  Writes out_id/out_meta[0..O) in the reference's order; returns O.
+// to t1 are dropped.  Writes out_id/out_meta[0..O) and returns O.  The reference orders
+// the outputs t1, negatives, t2; they are stored t1, t2, negatives, so that target 2 sits
+// at a fixed index (a run-time index into register arrays would put them in local
+// memory).  Every sum whose order matters walks them in the reference's order.
 __device__ __forceinline__ int select_outputs(const TrainParams& p, NegDraw nd, int t1, int t2, int* out_id,
                                               int* out_meta) {
   const int lane = lane_id();
@@ -213,15 +216,15 @@ __device__ __forceinline__ int select_outputs(const TrainParams& p, NegDraw nd, 
   const unsigned distinct = __ballot_sync(kFull, valid && leader && s != t1);
   const int O = __popc(distinct) + 2;
   if (valid && leader && s != t1) {
-    int idx = 1 + __popc(distinct & lanemask_lt());
+    int idx = 2 + __popc(distinct & lanemask_lt());
     out_id[idx] = s;
     out_meta[idx] = __popc(same);
   }
   if (lane == 0) {
     out_id[0] = t1;
     out_meta[0] = 1;
-    out_id[O - 1] = t2;
-    out_meta[O - 1] = 1;
+    out_id[1] = t2;
+    out_meta[1] = 1;
   }
   __syncwarp();
   return O;
@@ -406,7 +409,7 @@ __device__ __forceinline__ void forward_gradient_split8(int I, int first, int O,
 #pragma unroll
       for (int i = 0; i < OM; i++) {
         if (i < O) {
-          const int label = j < first ? (i == 0) : (i == O - 1);
+          const int label = j < first ? (i == 0) : (i == 1);  // outputs t1, t2, negatives
           const float s0 = __fadd_rn(f[i][0].x, f[i][0].y), s1 = __fadd_rn(f[i][1].x, f[i][1].y);
           const float s2 = __fadd_rn(f[i][2].x, f[i][2].y), s3 = __fadd_rn(f[i][3].x, f[i][3].y);
           const float fi = __fadd_rn(__fadd_rn(s0, s1), __fadd_rn(s2, s3));
@@ -456,7 +459,9 @@ __device__ __forceinline__ void store_out_normal(const float4 (&v)[OM][DCH], int
 // md is complete before any input row changes, as the reference's two GEMMs read the
 // same pre-update inputM.  apply_in(j, q, a) consumes input j's update of chunk q.
 // out_pair(p, q, r0, r1): rows 2p and 2p+1 of the step's outputs, columns 4q..4q+3.
-template <int OM, int DCH, class InPtr, class OutPair, class ApplyIn>
+// kT2Second: outputs are stored t1, t2, negatives (select_outputs); the sum over i still
+// runs in the reference's order t1, negatives, t2, i.e. stored rows 0, 2..O-1, 1.
+template <int OM, int DCH, bool kT2Second = false, class InPtr, class OutPair, class ApplyIn>
 __device__ __forceinline__ void backward(int I, int O, int d, InPtr in_ptr, OutPair out_pair,
                                          const float2* corrP, float4 (&md)[OM][DCH], ApplyIn apply_in) {
   typedef StepShape<OM> SS;
@@ -531,14 +536,18 @@ __device__ __forceinline__ void backward(int I, int O, int d, InPtr in_ptr, OutP
 #pragma unroll
         for (int u = 0; u < 4; u++) al[u] = ah[u] = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int i = 0; i < OM; i++)
-          if (i < O) {
+        for (int k = 0; k < OM; k++) {
+          // k-th term in the reference's order, as a stored row index (t2 comes last)
+          const int i = !kT2Second ? k : (k == 0 ? 0 : (k == OM - 1 ? 1 : k + 1));
+          const bool used = !kT2Second ? k < O : (k == 0 || k == OM - 1 || k + 1 < O);
+          if (used) {
 #pragma unroll
             for (int u = 0; u < 4; u++) {
               al[u] = ffma2(c[u][i], olo[i][t], al[u]);
               ah[u] = ffma2(c[u][i], ohi[i][t], ah[u]);
             }
           }
+        }
 #pragma unroll
         for (int u = 0; u < 4; u++)
           if (j0 + u < I) apply_in(j0 + u, q, make_float4(al[u].x, al[u].y, ah[u].x, ah[u].y));

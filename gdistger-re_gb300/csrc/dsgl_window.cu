@@ -344,7 +344,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
       r1 = 2 * pp + 1 < O ? reinterpret_cast<const float4*>(out_rows + (size_t)(2 * pp + 1) * DP)[q]
                           : make_float4(0.f, 0.f, 0.f, 0.f);
     };
-    backward<OM, DCH>(I, O, d, in_ptr, out_pair, corrP, md, add_to_input(in_ptr));
+    backward<OM, DCH, true>(I, O, d, in_ptr, out_pair, corrP, md, add_to_input(in_ptr));
     {  // Woh += outputMd: target 1, target 2, then each negative (aliases follow that order)
       uint64_t e1 = 0, e2 = 0, en = 0;
       if (S == STORE_BF16) {
@@ -357,18 +357,14 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
       for (int t = 0; t < DCH; t++) {
         const int q = lane + 32 * t;
         if (q < d4) {
-          float4 mlast = md[0][t];
-#pragma unroll
-          for (int i = 1; i < OM; i++)
-            if (i == O - 1) mlast = md[i][t];
+          // outputs are stored t1, t2, negatives (see select_outputs)
           const float4 b1 = reinterpret_cast<const float4*>(out_rows)[q];
           const float4 n1 = RowIO<S>::store4(p.woh, t1, d, q, add4(b1, md[0][t]), e1);
-          const float4 blast =
-              t2 == t1 ? n1 : reinterpret_cast<const float4*>(out_rows + (size_t)(O - 1) * DP)[q];
-          const float4 n2 = RowIO<S>::store4(p.woh, t2, d, q, add4(blast, mlast), e2);
+          const float4 b2 = t2 == t1 ? n1 : reinterpret_cast<const float4*>(out_rows + DP)[q];
+          const float4 n2 = RowIO<S>::store4(p.woh, t2, d, q, add4(b2, md[1][t]), e2);
 #pragma unroll
-          for (int i = 1; i < OM - 1; i++) {
-            if (i < O - 1) {
+          for (int i = 2; i < OM; i++) {
+            if (i < O) {
               const int row = out_id[i];
               const float4 bi = row == t2 ? n2 : reinterpret_cast<const float4*>(out_rows + (size_t)i * DP)[q];
               RowIO<S>::store4(p.woh, row, d, q, add4(bi, md[i][t]), en);
