@@ -260,7 +260,9 @@ __device__ __forceinline__ int select_outputs_stored(int K, const int* words, in
 // ---- window input list (dsgl.hpp:1100-1132) ------------------------------------------
 // Appends the positions c = pos - w + i, i in [b, 2w+1-b), i != w, 0 <= c < len in
 // increasing order; slot_of(c) gives the row index stored in in_row.  Returns the count.
-template <class SlotOf>
+// kEveryLane: slot_of is called by all 32 lanes (it may be a warp shuffle) with any c,
+// valid or not, and must be safe for every c; otherwise only for valid positions.
+template <bool kEveryLane = false, class SlotOf>
 __device__ __forceinline__ int window_inputs(int pos, int len, int w, int b, int base, int* in_row,
                                              SlotOf slot_of) {
   const int lane = lane_id();
@@ -270,7 +272,12 @@ __device__ __forceinline__ int window_inputs(int pos, int len, int w, int b, int
     const int c = pos - w + i;
     const bool ok = i >= b && i < 2 * w + 1 - b && i != w && c >= 0 && c < len;
     const unsigned m = __ballot_sync(kFull, ok);
-    if (ok) in_row[base + n + __popc(m & lanemask_lt())] = slot_of(c);
+    if (kEveryLane) {
+      const int sl = slot_of(c);
+      if (ok) in_row[base + n + __popc(m & lanemask_lt())] = sl;
+    } else {
+      if (ok) in_row[base + n + __popc(m & lanemask_lt())] = slot_of(c);
+    }
     n += __popc(m);
   }
   return n;

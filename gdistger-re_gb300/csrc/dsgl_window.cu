@@ -9,7 +9,9 @@
 //     [pos-w, pos+w] -- one fp32 copy per distinct vertex per walk, exactly the
 //     reference's per-walk deduplicated buffer, loaded when it enters the window and
 //     written back (stochastically rounded for bf16 tables) when it leaves it,
-//   * the step's output rows (target of each walk + shared negatives) and gradients.
+//   * the step's output rows (target of each walk + shared negatives) and gradients;
+// the window bookkeeping (vertex and count of each slot, slot of each position) lives in
+// registers, one slot per lane.
 // Negative rows are read from and added to Woh at each step, as the reference does for
 // the two target rows (dsgl.hpp:1346-1356).  Dot products of the forward are summed as
 // eight sequential partial sums (even and odd k of each quarter of [0, d)) combined
@@ -27,15 +29,19 @@ namespace {
 
 constexpr int kHdrWords = 1004 + 132;  // sigmoid table (1001 -> 1004) + SmallJumps (528 B)
 
+// Ring of position -> slot per walk, one entry per lane: position p's entry is held by
+// lane p & 31, and at most 2w + 2 positions are in a window at once.
+constexpr int kRing = 32;
+static_assert(kRing >= 2 * (kWMax - 1) + 2, "the ring must hold 2w + 2 positions for every allowed window");
+
 struct WinLayout {  // per-warp shared memory, in 4-byte words
-  int NS, R, DP, OP, OM, IM, lmax, outI;
-  int rows, corr, sen, vert, ref, ring, inrow, outid, outmeta, pend, words;
+  int NS, DP, OP, OM, IM, lmax, outI;
+  int rows, corr, sen, inrow, outid, outmeta, pend, words;
 };
 
 __host__ __device__ inline WinLayout win_layout(int d, int w, int K, int lmax) {
   WinLayout L;
   L.NS = 2 * w + 2;  // resident slots per walk (2w+1 positions, +1 while a row enters)
-  L.R = 2 * w + 2;   // ring of position -> slot
   L.DP = d + 4;      // padded row stride: 32 lanes reading 32 rows hit 32 distinct banks
   L.OM = K <= 5 ? 7 : kOMax;  // the kernel variant's output capacity (K + 2 <= OM)
   L.OP = (L.OM + 1) & ~1;     // outputs rounded up to pairs
@@ -50,12 +56,6 @@ __host__ __device__ inline WinLayout win_layout(int d, int w, int K, int lmax) {
   off += L.IM * (L.OP + 2) * 2;
   L.sen = off;
   off += 2 * lmax;
-  L.vert = off;
-  off += 2 * L.NS;
-  L.ref = off;
-  off += 2 * L.NS;
-  L.ring = off;
-  off += 2 * L.R;
   L.inrow = off;
   off += L.IM;
   L.outid = off;
@@ -137,15 +137,12 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
   float* out_rows = base + L.outI;
   float2* corrP = reinterpret_cast<float2*>(base + L.corr);
   int* sen = reinterpret_cast<int*>(base + L.sen);
-  int* vert = reinterpret_cast<int*>(base + L.vert);
-  int* ref = reinterpret_cast<int*>(base + L.ref);
-  int* ring = reinterpret_cast<int*>(base + L.ring);
   int* in_row = reinterpret_cast<int*>(base + L.inrow);
   int* out_id = reinterpret_cast<int*>(base + L.outid);
   int* out_meta = reinterpret_cast<int*>(base + L.outmeta);
   int* pend_id = reinterpret_cast<int*>(base + L.pend);
   int* pend_row = pend_id + (w + 1);
-  const int NS = L.NS, R = L.R, DP = L.DP, lmax = L.lmax;
+  const int NS = L.NS, DP = L.DP, lmax = L.lmax;
 
   // dsgl.hpp:790-826
   uint64_t rng = (uint64_t)wid, word_count = 0, last_wc = 0, step_id = 0;
@@ -157,10 +154,10 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
   int64_t cur = start;
   int local_iter = p.iter;
   int len[2] = {0, 0}, pos[2] = {0, 0};
-  int train_sen_num = 0, neg_count = 0, neg_n = 1, grp_g = -1;
+  // neg_g tracks neg_count % neg_n (the group of the step) without a division per step
+  int train_sen_num = 0, neg_count = 0, neg_n = 1, neg_g = 0, grp_g = -1;
   bool change_neg = true;
   uint64_t pool_base = 0, grp_state = 0;
-  for (int s = lane; s < 2 * NS; s += 32) ref[s] = 0;
   float loss = 0.f;
   unsigned long long n_pairs = 0, n_steps = 0, n_outs = 0, n_loads = 0, n_stores = 0;
   // negatives of the next step, drawn one step ahead when the pool stays (pf_g >= 0)
@@ -173,19 +170,23 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
   int ent_row[2] = {-1, -1};
   __syncwarp();
 
+  // The window slot tables live in registers: lane s holds, for each walk, the vertex of
+  // slot s (sv), its count of window positions (sr; 0 = free) and, for the position p
+  // with p & 31 == lane, the slot p is assigned to (rg).  Walk indices are run-time values
+  // in some loops, so the per-walk copies are separate scalars selected by walk.
+  int sv0 = 0, sv1 = 0, sr0 = 0, sr1 = 0, rg0 = 0, rg1 = 0;
   // Places position `position` of walk `walk` in the window: an existing slot of the same
-  // vertex, or a free slot.  Returns the slot; *fresh says the row must be loaded.
-  auto enter_assign = [&](int walk, int position, bool* fresh_out) -> int {
+  // vertex, or a free slot.  Returns the slot; *fresh says row *v_out must be loaded.
+  auto enter_assign = [&](int walk, int position, bool* fresh_out, int* v_out) -> int {
     const int v = sen[walk * lmax + position];
-    int* wref = ref + walk * NS;
-    int* wvert = vert + walk * NS;
-    const unsigned hit = __ballot_sync(kFull, lane < NS && wref[lane] > 0 && wvert[lane] == v);
+    const int my_v = walk ? sv1 : sv0, my_r = walk ? sr1 : sr0;
+    const unsigned hit = __ballot_sync(kFull, lane < NS && my_r > 0 && my_v == v);
     int s;
     bool fresh = false;
     if (hit) {
       s = __ffs(hit) - 1;
     } else {
-      const unsigned fr = __ballot_sync(kFull, lane < NS && wref[lane] == 0);
+      const unsigned fr = __ballot_sync(kFull, lane < NS && my_r == 0);
       s = __ffs(fr) - 1;
       fresh = true;
       if (s < 0) {  // cannot happen: at most 2w+2 distinct vertices are resident
@@ -193,14 +194,14 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
         s = 0;
       }
     }
-    __syncwarp();
-    if (lane == 0) {
-      if (fresh) wvert[s] = v;
-      wref[s] += 1;
-      ring[walk * R + position % R] = s;
+    if (lane == s) {
+      if (walk) { sv1 = v; sr1 = my_r + 1; } else { sv0 = v; sr0 = my_r + 1; }
     }
-    __syncwarp();
+    if (lane == (position & (kRing - 1))) {
+      if (walk) rg1 = s; else rg0 = s;
+    }
     *fresh_out = fresh;
+    *v_out = v;
     return s;
   };
   // the first window of a freshly loaded walk: slots first, then one batched load
@@ -208,10 +209,11 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     int n = 0;
     for (int q = 0; q <= hi; q++) {
       bool fresh;
-      const int s = enter_assign(walk, q, &fresh);
+      int v;
+      const int s = enter_assign(walk, q, &fresh, &v);
       if (fresh) {
         if (lane == 0) {
-          pend_id[n] = vert[walk * NS + s];
+          pend_id[n] = v;
           pend_row[n] = walk * NS + s;
         }
         n++;
@@ -223,28 +225,27 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     __syncwarp();
   };
   auto leave = [&](int walk, int position, uint64_t ev) {
-    const int s = ring[walk * R + position % R];
-    const int r = ref[walk * NS + s] - 1;
-    const int v = vert[walk * NS + s];
-    __syncwarp();
-    if (lane == 0) ref[walk * NS + s] = r;
+    const int s = __shfl_sync(kFull, walk ? rg1 : rg0, position & (kRing - 1));
+    const int r = __shfl_sync(kFull, walk ? sr1 : sr0, s) - 1;
+    const int v = __shfl_sync(kFull, walk ? sv1 : sv0, s);
+    if (lane == s) {
+      if (walk) sr1 = r; else sr0 = r;
+    }
     if (r == 0) {
       store_row_from_smem<S>(p.wih, v, d, rows + (size_t)(walk * NS + s) * DP, ev);
       n_stores++;
     }
-    __syncwarp();
   };
   auto flush_walk = [&](int walk, uint64_t ev) {
-    for (int s = 0; s < NS; s++) {
-      const int r = ref[walk * NS + s];
-      if (r > 0) {
-        store_row_from_smem<S>(p.wih, vert[walk * NS + s], d, rows + (size_t)(walk * NS + s) * DP, ev);
-        n_stores++;
-      }
+    const int my_r = walk ? sr1 : sr0, my_v = walk ? sv1 : sv0;
+    unsigned live = __ballot_sync(kFull, lane < NS && my_r > 0);
+    while (live) {
+      const int s = __ffs(live) - 1;
+      live &= live - 1;
+      store_row_from_smem<S>(p.wih, __shfl_sync(kFull, my_v, s), d, rows + (size_t)(walk * NS + s) * DP, ev);
+      n_stores++;
     }
-    __syncwarp();
-    for (int s = lane; s < NS; s += 32) ref[walk * NS + s] = 0;
-    __syncwarp();
+    if (walk) sr1 = 0; else sr0 = 0;
   };
 
   while (true) {
@@ -275,13 +276,13 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
       cur = start;
       len[0] = len[1] = 0;
       ent_row[0] = ent_row[1] = -1;
-      for (int s = lane; s < 2 * NS; s += 32) ref[s] = 0;
-      __syncwarp();
+      sr0 = sr1 = 0;
       continue;
     }
     if (change_neg) {  // dsgl.hpp:1054-1088: the pool is its base state and size
       pool_base = rng;
       neg_n = len[0] > len[1] ? len[0] : len[1];
+      neg_g = neg_count % neg_n;
       rng = jump_any(rng, (uint64_t)neg_n * (uint64_t)K, p.jumps);
       change_neg = false;
       grp_g = -1;
@@ -296,12 +297,13 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     const int t1 = sen[pos[0]], t2 = sen[lmax + pos[1]];
     rng = lcg_next(rng);
     const int b = (int)fast_mod(rng, p.div_window);
-    const int I0 = window_inputs(pos[0], len[0], w, b, 0, in_row,
-                                 [&](int c) { return ring[c % R]; });
-    const int I = I0 + window_inputs(pos[1], len[1], w, b, I0, in_row,
-                                     [&](int c) { return NS + ring[R + c % R]; });
+    const int I0 = window_inputs<true>(pos[0], len[0], w, b, 0, in_row,
+                                 [&](int c) { return __shfl_sync(kFull, rg0, c & (kRing - 1)); });
+    const int I = I0 + window_inputs<true>(pos[1], len[1], w, b, I0, in_row,
+                                     [&](int c) { return NS + __shfl_sync(kFull, rg1, c & (kRing - 1)); });
     neg_count++;
-    const int g = neg_count % neg_n;
+    neg_g = neg_g + 1 == neg_n ? 0 : neg_g + 1;
+    const int g = neg_g;
     NegDraw nd;
     if (g == pf_g) {
       nd = pf;
@@ -398,9 +400,9 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
           const int P = pos[walk];
           if (P + w < len[walk]) {
             bool fresh;
-            const int s = enter_assign(walk, P + w, &fresh);
+            int v;
+            const int s = enter_assign(walk, P + w, &fresh, &v);
             if (fresh) {
-              const int v = vert[walk * NS + s];
 #pragma unroll
               for (int t = 0; t < DCH; t++) {
                 const int q = lane + 32 * t;
@@ -419,7 +421,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
       train_sen_num = 0;
     }
     if (!change_neg) {  // the pool stays: draw the next step's negatives now
-      const int gn = (neg_count + 1) % neg_n;
+      const int gn = neg_g + 1 == neg_n ? 0 : neg_g + 1;
       uint64_t gs;
       if (gn == 0) gs = pool_base;
       else if (gn == grp_g + 1) gs = jump_small(grp_state, K, *sj);
