@@ -295,12 +295,6 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     const uint64_t sr_key =
         S == STORE_BF16 && lane <= EV_NEG ? sr_event_key(p.sr_seed, lane, (uint32_t)wid, step_id) : 0;
     const int t1 = sen[pos[0]], t2 = sen[lmax + pos[1]];
-    rng = lcg_next(rng);
-    const int b = (int)fast_mod(rng, p.div_window);
-    const int I0 = window_inputs<true>(pos[0], len[0], w, b, 0, in_row,
-                                 [&](int c) { return __shfl_sync(kFull, rg0, c & (kRing - 1)); });
-    const int I = I0 + window_inputs<true>(pos[1], len[1], w, b, I0, in_row,
-                                     [&](int c) { return NS + __shfl_sync(kFull, rg1, c & (kRing - 1)); });
     neg_count++;
     neg_g = neg_g + 1 == neg_n ? 0 : neg_g + 1;
     const int g = neg_g;
@@ -318,11 +312,32 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     }
     grp_g = g;
     const int O = select_outputs(p, nd, t1, t2, out_id, out_meta);
-    {  // gather the output rows (targets and negatives) from Woh, all loads in flight at once
-      float4 v[OM][DCH];
-      load_out_rows<S, OM, DCH>(p.woh, out_id, O, d, v);
-      store_out_normal<OM, DCH>(v, O, d, out_rows, DP);
+    // Gather the output rows (targets and negatives) from Woh: every load is issued here and
+    // kept raw; the window input lists are built while they are in flight.
+    const int d4 = d >> 2;
+    typename RowIO<S>::Raw ov[OM][DCH];
+#pragma unroll
+    for (int i = 0; i < OM; i++) {
+      const int row = i < O ? out_id[i] : 0;
+#pragma unroll
+      for (int t = 0; t < DCH; t++) {
+        const int q = lane + 32 * t;
+        ov[i][t] = (i < O && q < d4) ? RowIO<S>::load_raw(p.woh, row, d, q) : typename RowIO<S>::Raw{};
+      }
     }
+    rng = lcg_next(rng);
+    const int b = (int)fast_mod(rng, p.div_window);
+    const int I0 = window_inputs<true>(pos[0], len[0], w, b, 0, in_row,
+                                 [&](int c) { return __shfl_sync(kFull, rg0, c & (kRing - 1)); });
+    const int I = I0 + window_inputs<true>(pos[1], len[1], w, b, I0, in_row,
+                                     [&](int c) { return NS + __shfl_sync(kFull, rg1, c & (kRing - 1)); });
+#pragma unroll
+    for (int i = 0; i < OM; i++)
+#pragma unroll
+      for (int t = 0; t < DCH; t++) {
+        const int q = lane + 32 * t;
+        if (i < O && q < d4) reinterpret_cast<float4*>(out_rows + (size_t)i * DP)[q] = RowIO<S>::widen(ov[i][t]);
+      }
 #pragma unroll
     for (int walk = 0; walk < 2; walk++) {
       if (ent_row[walk] >= 0) {
