@@ -45,6 +45,7 @@ NCU_DRAM_BYTES_PER_PAIR = {"lj-cl": 1429.11e9 / 7597249326, "small": 50.27e9 / 6
 WORKLOADS = {
     "lj-cl": dict(V=2238731, E=30_000_000, gamma=2.1, walks=10, mean=40, cap=80),
     "small": dict(V=200_000, E=2_000_000, gamma=2.1, walks=10, mean=40, cap=80),
+    "tiny": dict(V=5_000, E=50_000, gamma=2.1, walks=10, mean=40, cap=80),  # test-sized
 }
 TRAIN = dict(size=128, window=10, negative=5, sample=1e-3, alpha=0.01, table_size=100_000_000, threads=12)
 

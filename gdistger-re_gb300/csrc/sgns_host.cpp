@@ -158,6 +158,10 @@ sgns_status validate(sgns_handle* h, const sgns_options& o) {
     return fail(h, SGNS_EINVAL, "unknown engine %d", o.engine);
   if (o.workers < 0 || o.warps_per_cta < 0 || o.warps_per_cta > 8)
     return fail(h, SGNS_EINVAL, "workers/warps_per_cta out of range");
+  if (o.mode != SGNS_MODE_HOGWILD && o.mode != SGNS_MODE_REPLAY_EXACT)
+    return fail(h, SGNS_EINVAL, "unknown mode %d", o.mode);
+  if (o.mode == SGNS_MODE_REPLAY_EXACT && o.workers > 1)
+    return fail(h, SGNS_EINVAL, "-mode exact replays one worker; -workers %d asks for more", o.workers);
   return SGNS_OK;
 }
 
@@ -496,6 +500,12 @@ sgns_status sgns_options_from_args(sgns_options* o, int argc, const char* const*
     else if (!std::strcmp(argv[i + 1], "bf16")) o->storage = SGNS_STORE_BF16_SR;
     else return fail(nullptr, SGNS_EINVAL, "-storage %s: expected fp32 or bf16", argv[i + 1]);
   }
+  if ((i = pos("-mode")) > 0) {
+    if (i + 1 >= argc) return fail(nullptr, SGNS_EINVAL, "flag -mode needs a value");
+    if (!std::strcmp(argv[i + 1], "hogwild")) o->mode = SGNS_MODE_HOGWILD;
+    else if (!std::strcmp(argv[i + 1], "exact")) o->mode = SGNS_MODE_REPLAY_EXACT;
+    else return fail(nullptr, SGNS_EINVAL, "-mode %s: expected hogwild or exact", argv[i + 1]);
+  }
   if ((i = pos("-engine")) > 0) {
     if (i + 1 >= argc) return fail(nullptr, SGNS_EINVAL, "flag -engine needs a value");
     if (!std::strcmp(argv[i + 1], "plain")) o->engine = SGNS_ENGINE_PLAIN;
@@ -690,13 +700,24 @@ sgns_status sgns_train(sgns_handle* h) {
   float ms = 0.f;
   int workers = 0;
   sgns_status st;
+  const bool exact = h->opt.mode == SGNS_MODE_REPLAY_EXACT;
   if (h->opt.engine == SGNS_ENGINE_PERSISTENT) {
+    if (exact) {  // one worker in a one-warp CTA: nothing to tune
+      workers = 1;
+      h->wpc = h->opt.warps_per_cta > 0 ? h->opt.warps_per_cta : 1;
+      st = run_persistent(h, 1, h->wpc, true, &ms);
+      if (st) return st;
+      return finish_stats(h, workers, ms);
+    }
     if (!h->tuned) {
       st = autotune(h);
       if (st) return st;
     }
     workers = h->opt.workers > 0 ? h->opt.workers : h->workers;
     st = run_persistent(h, workers, h->wpc, true, &ms);
+  } else if (exact) {
+    workers = 1;
+    st = run_plain(h, 1, &ms);
   } else {
     // Default worker count.  Each worker of the reference policy holds snapshots of about
     // max(len1,len2)*K negative rows and two walks' rows and writes them back over the

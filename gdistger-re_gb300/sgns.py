@@ -17,6 +17,7 @@ HEADER = os.path.join(ROOT, "include", "sgns.h")
 OK, EINVAL, ENOMEM, ECUDA, ETIMEOUT, EIO, ESTATE = range(7)
 STORE_FP32, STORE_BF16_SR = 0, 1
 ENGINE_PLAIN, ENGINE_PERSISTENT = 0, 1
+MODE_HOGWILD, MODE_REPLAY_EXACT = 0, 1
 
 
 class Options(ctypes.Structure):
@@ -26,7 +27,7 @@ class Options(ctypes.Structure):
         ("min_count", ctypes.c_int32), ("iter", ctypes.c_int32), ("threads", ctypes.c_int32),
         ("debug", ctypes.c_int32), ("binary", ctypes.c_int32), ("storage", ctypes.c_int32),
         ("engine", ctypes.c_int32), ("workers", ctypes.c_int32), ("warps_per_cta", ctypes.c_int32),
-        ("device", ctypes.c_int32), ("compute_loss", ctypes.c_int32), ("reserved0", ctypes.c_int32),
+        ("device", ctypes.c_int32), ("compute_loss", ctypes.c_int32), ("mode", ctypes.c_int32),
         ("table_size", ctypes.c_int64), ("seed", ctypes.c_uint64),
     ]
 
@@ -54,7 +55,7 @@ _lib = None
 
 def header_functions():
     """Names of the functions include/sgns.h declares."""
-    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", " ", open(HEADER).read(), flags=re.S)  # declarations only, not comments
     return sorted(set(re.findall(r"\b(sgns_[a-z_0-9]+)\s*\(", text)))
 
 
@@ -111,6 +112,8 @@ def default_options(**kw):
             v = {"fp32": STORE_FP32, "bf16": STORE_BF16_SR}[v]
         if k == "engine" and isinstance(v, str):
             v = {"plain": ENGINE_PLAIN, "persistent": ENGINE_PERSISTENT}[v]
+        if k == "mode" and isinstance(v, str):
+            v = {"hogwild": MODE_HOGWILD, "exact": MODE_REPLAY_EXACT}[v]
         setattr(o, k, v)
     return o
 

@@ -49,6 +49,16 @@ typedef enum sgns_engine {
   SGNS_ENGINE_PERSISTENT = 1
 } sgns_engine;
 
+typedef enum sgns_mode {
+  /* Workers train concurrently and write the shared tables without locks, as the
+   * reference's compute threads do (dsgl.hpp:1352-1356, 1380-1404). */
+  SGNS_MODE_HOGWILD = 0,
+  /* One worker: a deterministic run that replays the reference's single-compute-thread
+   * order, bit for bit with the CPU oracle (and, for the plain engine, with the
+   * reference itself).  workers must be 0 or 1. */
+  SGNS_MODE_REPLAY_EXACT = 1
+} sgns_mode;
+
 typedef struct sgns_options {
   int32_t size;        /* -size       hidden size d (multiple of 4, <= 256)       */
   int32_t window;      /* -window     w (1..16)                                   */
@@ -67,7 +77,7 @@ typedef struct sgns_options {
   int32_t warps_per_cta; /* persistent engine CTA shape; 0 = tuned                */
   int32_t device;      /* CUDA device ordinal                                     */
   int32_t compute_loss;/* 1 = also accumulate the SGNS loss (fp64 reduction)      */
-  int32_t reserved0;
+  int32_t mode;        /* sgns_mode (-mode hogwild|exact)                         */
   int64_t table_size;  /* unigram table entries (the reference fixes 1e8, dsgl.hpp:82) */
   uint64_t seed;       /* stochastic-rounding stream seed                         */
 } sgns_options;
@@ -91,7 +101,7 @@ typedef struct sgns_stats {
 void sgns_default_options(sgns_options* opt);
 /* Fills opt from word2vec-style flags exactly as dsgl.hpp:1495-1535 scans them
  * (unknown flags ignored).  Adds -storage fp32|bf16, -engine plain|persistent,
- * -workers N, -table-size N, -seed N. */
+ * -mode hogwild|exact, -workers N, -table-size N, -seed N. */
 sgns_status sgns_options_from_args(sgns_options* opt, int argc, const char* const* argv);
 
 typedef struct sgns_handle sgns_handle;

@@ -46,8 +46,18 @@ def test_bad_storage_name(sgns_lib):
         sgns.options_from_args(["-storage", "fp8"])
 
 
+def test_mode_flag(sgns_lib):
+    assert sgns.default_options().mode == sgns.MODE_HOGWILD
+    assert sgns.options_from_args(["-mode", "exact"]).mode == sgns.MODE_REPLAY_EXACT
+    assert sgns.options_from_args(["-mode", "hogwild"]).mode == sgns.MODE_HOGWILD
+    with pytest.raises(sgns.SgnsError) as e:
+        sgns.options_from_args(["-mode", "lockstep"])
+    assert e.value.status == sgns.EINVAL
+
+
 def test_invalid_options_rejected_before_device(sgns_lib):
-    for kw in (dict(size=130), dict(size=512), dict(window=0), dict(window=16), dict(negative=11), dict(iter=0)):
+    for kw in (dict(size=130), dict(size=512), dict(window=0), dict(window=16), dict(negative=11), dict(iter=0),
+               dict(mode=2), dict(mode="exact", workers=2)):
         with pytest.raises(sgns.SgnsError) as e:
             sgns.Trainer(**kw)
         assert e.value.status == sgns.EINVAL

@@ -63,12 +63,12 @@ def case(name):
     return cfg, corpus.astype(np.int32), None
 
 
-def gpu_train(cfg, corpus, engine, storage, workers=1, wpc=1, table_size=None, table_threads=2):
+def gpu_train(cfg, corpus, engine, storage, workers=1, wpc=1, table_size=None, table_threads=2, mode="hogwild"):
     counts = np.bincount(corpus[corpus >= 0], minlength=cfg["V"]).astype(np.int32)
     opt = sgns.default_options(size=cfg["d"], window=cfg["window"], negative=cfg["negative"], iter=cfg["iter"],
                                sample=cfg["sample"], alpha=cfg["alpha"], engine=engine, storage=storage,
                                workers=workers, warps_per_cta=wpc, threads=table_threads,
-                               table_size=table_size or 1000000, debug=0)
+                               table_size=table_size or 1000000, debug=0, mode=mode)
     with sgns.Trainer(opt) as t:
         t.set_vocab(counts)
         st = t.train_corpus(corpus)
@@ -116,6 +116,26 @@ def test_persistent_matches_oracle(name, storage, wpc, sgns_lib, oracle_mod):
     owih, owoh, ost = oracle_train(oracle_mod, cfg, corpus, oracle_mod.POLICY_WINDOW, storage)
     assert (st.steps, st.pairs, st.word_count_actual) == (ost["steps"], ost["pairs"], ost["word_count_actual"])
     assert abs(st.final_alpha - ost["final_alpha"]) == 0
+    assert np.array_equal(wih.view(np.uint32), owih.view(np.uint32)), np.abs(wih - owih).max()
+    assert np.array_equal(woh.view(np.uint32), owoh.view(np.uint32)), np.abs(woh - owoh).max()
+
+
+@pytest.mark.parametrize("engine,storage", [("plain", "fp32"), ("persistent", "fp32"), ("persistent", "bf16")])
+def test_replay_exact_mode_on_the_10k_vertex_case(engine, storage, sgns_lib, oracle_mod):
+    """Replay-exact mode (no worker count given) on a 10,000-vertex Chung-Lu graph
+    (98k edges, gamma 2.1), one uniform walk of 80 per vertex (0.8M tokens), d=128, w=10,
+    K=5, sample 1e-3, alpha 0.01, unigram table 1e7: one worker, bit for bit the oracle."""
+    import synth
+
+    ip, ix = synth.chung_lu(10000, 100000, 2.1, seed=1001)
+    corpus = synth.random_walks(ip, ix, 1, 80, seed=1002).numpy().astype(np.int32)
+    cfg = dict(V=10000, d=128, window=10, negative=5, iter=1, sample=1e-3, alpha=0.01)
+    wih, woh, st, _ = gpu_train(cfg, corpus, engine, storage, workers=0, wpc=0, table_size=10_000_000,
+                                mode="exact")
+    policy = oracle_mod.POLICY_REF if engine == "plain" else oracle_mod.POLICY_WINDOW
+    owih, owoh, ost = oracle_train(oracle_mod, cfg, corpus, policy, storage, table_size=10_000_000)
+    assert st.workers == 1
+    assert (st.steps, st.pairs, st.word_count_actual) == (ost["steps"], ost["pairs"], ost["word_count_actual"])
     assert np.array_equal(wih.view(np.uint32), owih.view(np.uint32)), np.abs(wih - owih).max()
     assert np.array_equal(woh.view(np.uint32), owoh.view(np.uint32)), np.abs(woh - owoh).max()
 
