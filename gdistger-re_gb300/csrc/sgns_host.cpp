@@ -660,24 +660,11 @@ sgns_status sgns_reset_model(sgns_handle* h) {
   return SGNS_OK;
 }
 
-sgns_status sgns_upload_corpus(sgns_handle* h, const int32_t* tokens, int64_t n) {
-  if (!h || (!tokens && n > 0) || n < 0) return fail(h, SGNS_EINVAL, "bad corpus arguments");
-  if (!h->wih) return fail(h, SGNS_ESTATE, "sgns_set_vocab has not been called");
-  CU(h, cudaSetDevice(h->opt.device));
-  if (n > h->corpus_cap) {
-    dfree(h->d_ids);
-    dfree(h->d_corpus);
-    h->corpus_cap = 0;
-    cudaError_t e;
-    if ((e = cudaMalloc(&h->d_ids, sizeof(int32_t) * n)) != cudaSuccess ||
-        (e = cudaMalloc(&h->d_corpus, sizeof(int32_t) * n)) != cudaSuccess)
-      return fail(h, SGNS_ENOMEM, "corpus of %lld tokens: %s", (long long)n, cudaGetErrorString(e));
-    h->corpus_cap = n;
-  }
+// Maps the n ids in h->d_ids to sorted rows (validating them), finds the longest walk.
+sgns_status map_uploaded_corpus(sgns_handle* h, int64_t n) {
   h->n_tokens = n;
   CU(h, cudaMemsetAsync(h->d_flags, 0, 4 * sizeof(int32_t), h->stream));
   if (n > 0) {
-    CU(h, cudaMemcpyAsync(h->d_ids, tokens, sizeof(int32_t) * n, cudaMemcpyHostToDevice, h->stream));
     CU(h, launch_map_corpus(h->d_ids, h->d_row_of, h->d_corpus, n, h->V, h->d_flags, h->stream));
     CU(h, launch_max_walk(h->d_corpus, n, h->d_flags + 1, h->stream));
   }
@@ -691,6 +678,29 @@ sgns_status sgns_upload_corpus(sgns_handle* h, const int32_t* tokens, int64_t n)
   if (lmax != h->lmax) h->tuned = false;
   h->lmax = lmax;
   return SGNS_OK;
+}
+
+sgns_status ensure_corpus_capacity(sgns_handle* h, int64_t n) {
+  if (n <= h->corpus_cap) return SGNS_OK;
+  dfree(h->d_ids);
+  dfree(h->d_corpus);
+  h->corpus_cap = 0;
+  cudaError_t e;
+  if ((e = cudaMalloc(&h->d_ids, sizeof(int32_t) * n)) != cudaSuccess ||
+      (e = cudaMalloc(&h->d_corpus, sizeof(int32_t) * n)) != cudaSuccess)
+    return fail(h, SGNS_ENOMEM, "corpus of %lld tokens: %s", (long long)n, cudaGetErrorString(e));
+  h->corpus_cap = n;
+  return SGNS_OK;
+}
+
+sgns_status sgns_upload_corpus(sgns_handle* h, const int32_t* tokens, int64_t n) {
+  if (!h || (!tokens && n > 0) || n < 0) return fail(h, SGNS_EINVAL, "bad corpus arguments");
+  if (!h->wih) return fail(h, SGNS_ESTATE, "sgns_set_vocab has not been called");
+  CU(h, cudaSetDevice(h->opt.device));
+  sgns_status st = ensure_corpus_capacity(h, n);
+  if (st) return st;
+  if (n > 0) CU(h, cudaMemcpyAsync(h->d_ids, tokens, sizeof(int32_t) * n, cudaMemcpyHostToDevice, h->stream));
+  return map_uploaded_corpus(h, n);
 }
 
 sgns_status sgns_train(sgns_handle* h) {
@@ -850,59 +860,162 @@ sgns_status sgns_save_text(sgns_handle* h, const char* path) {
   return SGNS_OK;
 }
 
+namespace {
+// Parses n bytes of walk text in device memory into tokens (capacity cap); see
+// sgns_parse_walks.  h may be null (kernel-level call).
+sgns_status parse_walks(sgns_handle* h, const uint8_t* bytes, int64_t n, int32_t* tokens, int64_t cap,
+                        int64_t* n_tokens, int64_t* max_id, cudaStream_t s) {
+  DeviceScratch* ds = device_scratch();
+  if (!ds) return fail(h, SGNS_ECUDA, "no current CUDA device");
+  std::lock_guard<std::mutex> g(ds->mx);
+  sgns_status st = ds->ensure(ingest_scratch_bytes(n));
+  if (st) return st;
+  unsigned long long cnt = 0;
+  long long err = 0, mx = -1;
+  cudaError_t e = launch_ingest_count(bytes, n, ds->buf, &cnt, &err, s);
+  if (e != cudaSuccess) return fail(h, SGNS_ECUDA, "walk parse: %s", cudaGetErrorString(e));
+  if (err != 0x7FFFFFFFFFFFFFFFLL) {
+    uint8_t c = 0;
+    cudaMemcpy(&c, bytes + err, 1, cudaMemcpyDeviceToHost);
+    return fail(h, SGNS_EINVAL, "unexpected byte 0x%02x at offset %lld of the walk text", c, err);
+  }
+  *n_tokens = (int64_t)cnt;
+  *max_id = -1;
+  if ((int64_t)cnt > cap)
+    return fail(h, SGNS_EINVAL, "walk text yields %llu tokens, capacity %lld", cnt, (long long)cap);
+  if (cnt == 0) return SGNS_OK;
+  e = launch_ingest_emit(bytes, n, ds->buf, tokens, &err, &mx, s);
+  if (e != cudaSuccess) return fail(h, SGNS_ECUDA, "walk parse: %s", cudaGetErrorString(e));
+  if (err != 0x7FFFFFFFFFFFFFFFLL)
+    return fail(h, SGNS_EINVAL, "vertex id ending at offset %lld of the walk text exceeds 2^31 - 1", err);
+  *max_id = mx;
+  return SGNS_OK;
+}
+}  // namespace
+
+sgns_status sgns_parse_walks(const uint8_t* bytes, int64_t n, int32_t* tokens, int64_t cap, int64_t* n_tokens,
+                             int64_t* max_id, void* stream) {
+  if ((!bytes && n > 0) || n < 0 || cap < 0 || (cap > 0 && !tokens) || !n_tokens || !max_id)
+    return fail(nullptr, SGNS_EINVAL, "bad walk-parse arguments");
+  return parse_walks(nullptr, bytes, n, tokens, cap, n_tokens, max_id, static_cast<cudaStream_t>(stream));
+}
+
 sgns_status sgns_train_walk_files(sgns_handle* h, const char* const* paths, int32_t n_paths, int64_t V) {
   if (!h || !paths || n_paths <= 0) return fail(h, SGNS_EINVAL, "bad arguments");
-  std::vector<int32_t> tokens;
-  int64_t max_id = -1;
+  CU(h, cudaSetDevice(h->opt.device));
+  // total text: each file followed by a newline, which ends its last walk as the host
+  // reader did at end of file
+  std::vector<int64_t> sizes(n_paths);
+  int64_t total = 0;
   for (int p = 0; p < n_paths; p++) {
-    FILE* f = fopen(paths[p], "rb");
-    if (!f) return fail(h, SGNS_EIO, "cannot open walk file %s", paths[p]);
-    std::vector<char> buf(1 << 22);
-    int64_t cur = -1;  // value being parsed, -1 = none
-    bool line_has_tokens = false;
-    size_t got;
-    while ((got = fread(buf.data(), 1, buf.size(), f)) > 0) {
-      for (size_t i = 0; i < got; i++) {
-        const char c = buf[i];
-        if (c >= '0' && c <= '9') {
-          cur = (cur < 0 ? 0 : cur * 10) + (c - '0');
-          if (cur > INT32_MAX) {
-            fclose(f);
-            return fail(h, SGNS_EINVAL, "vertex id too large in %s", paths[p]);
-          }
-        } else if (c == ' ' || c == '\t' || c == '\r' || c == '\n') {
-          if (cur >= 0) {
-            tokens.push_back((int32_t)cur);
-            max_id = std::max(max_id, cur);
-            line_has_tokens = true;
-            cur = -1;
-          }
-          if (c == '\n' && line_has_tokens) {  // one walk per line (path.hpp:108-110)
-            tokens.push_back(-1);
-            line_has_tokens = false;
-          }
-        } else {
-          fclose(f);
-          return fail(h, SGNS_EINVAL, "unexpected byte 0x%02x in walk file %s", (unsigned char)c, paths[p]);
-        }
-      }
+    FILE* f = paths[p] ? fopen(paths[p], "rb") : nullptr;
+    if (!f) return fail(h, SGNS_EIO, "cannot open walk file %s", paths[p] ? paths[p] : "(null)");
+    if (fseek(f, 0, SEEK_END) != 0 || (sizes[p] = (int64_t)ftell(f)) < 0) {
+      fclose(f);
+      return fail(h, SGNS_EIO, "cannot size walk file %s", paths[p]);
     }
     fclose(f);
-    if (cur >= 0) {
-      tokens.push_back((int32_t)cur);
-      max_id = std::max(max_id, cur);
-      line_has_tokens = true;
-    }
-    if (line_has_tokens) tokens.push_back(-1);
+    total += sizes[p] + 1;
   }
+  uint8_t* d_text = nullptr;
+  uint8_t* stage[2] = {nullptr, nullptr};
+  cudaEvent_t done[2] = {nullptr, nullptr};
+  int32_t* d_tok = nullptr;
+  int32_t* d_cnt = nullptr;
+  auto cleanup = [&]() {
+    cudaStreamSynchronize(h->stream);
+    dfree(d_text);
+    for (int k = 0; k < 2; k++) {
+      if (stage[k]) cudaFreeHost(stage[k]);
+      if (done[k]) cudaEventDestroy(done[k]);
+    }
+    dfree(d_tok);
+    dfree(d_cnt);
+  };
+  auto bail = [&](sgns_status st) {
+    cleanup();
+    return st;
+  };
+  const size_t kStage = (size_t)64 << 20;
+  cudaError_t e;
+  if ((e = cudaMalloc(&d_text, (size_t)total)) != cudaSuccess)
+    return bail(fail(h, SGNS_ENOMEM, "walk text of %lld bytes: %s", (long long)total, cudaGetErrorString(e)));
+  for (int k = 0; k < 2; k++)
+    if ((e = cudaHostAlloc(&stage[k], kStage, cudaHostAllocDefault)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming)) != cudaSuccess)
+      return bail(fail(h, SGNS_ENOMEM, "staging buffers: %s", cudaGetErrorString(e)));
+  // read every file through two pinned staging buffers; the copy of one overlaps the read
+  // of the next
+  int64_t off = 0;
+  int k = 0;
+  bool used[2] = {false, false};
+  for (int p = 0; p < n_paths; p++) {
+    FILE* f = fopen(paths[p], "rb");
+    if (!f) return bail(fail(h, SGNS_EIO, "cannot open walk file %s", paths[p]));
+    int64_t left = sizes[p] + 1;
+    while (left > 0) {
+      if (used[k] && (e = cudaEventSynchronize(done[k])) != cudaSuccess) {
+        fclose(f);
+        return bail(fail(h, SGNS_ECUDA, "staging copy: %s", cudaGetErrorString(e)));
+      }
+      size_t want = (size_t)std::min<int64_t>(left, (int64_t)kStage), got = 0;
+      const bool last = (int64_t)want == left;  // this chunk ends with the file's newline
+      const size_t from_file = last ? want - 1 : want;
+      if (from_file > 0) got = fread(stage[k], 1, from_file, f);
+      if (got != from_file) {
+        fclose(f);
+        return bail(fail(h, SGNS_EIO, "short read of walk file %s", paths[p]));
+      }
+      if (last) stage[k][want - 1] = '\n';
+      if ((e = cudaMemcpyAsync(d_text + off, stage[k], want, cudaMemcpyHostToDevice, h->stream)) != cudaSuccess ||
+          (e = cudaEventRecord(done[k], h->stream)) != cudaSuccess) {
+        fclose(f);
+        return bail(fail(h, SGNS_ECUDA, "staging copy: %s", cudaGetErrorString(e)));
+      }
+      used[k] = true;
+      off += (int64_t)want;
+      left -= (int64_t)want;
+      k ^= 1;
+    }
+    fclose(f);
+  }
+  int64_t n = 0, max_id = -1;
+  sgns_status st = parse_walks(h, d_text, total, nullptr, 0, &n, &max_id, h->stream);
+  if (st && n == 0) return bail(st);  // a bad byte (a zero-token text is not an error here)
+  if (n > 0) {
+    if ((e = cudaMalloc(&d_tok, sizeof(int32_t) * (size_t)n)) != cudaSuccess)
+      return bail(fail(h, SGNS_ENOMEM, "corpus of %lld tokens: %s", (long long)n, cudaGetErrorString(e)));
+    st = parse_walks(h, d_text, total, d_tok, n, &n, &max_id, h->stream);
+    if (st) return bail(st);
+  }
+  dfree(d_text);
   if (V <= 0) V = max_id + 1;
-  if (max_id >= V) return fail(h, SGNS_EINVAL, "walk files name vertex %lld >= V = %lld", (long long)max_id, (long long)V);
-  std::vector<int32_t> counts(V, 0);  // vertex_cn, path.hpp:98
-  for (int32_t t : tokens)
-    if (t >= 0) counts[t]++;
-  sgns_status st = sgns_set_vocab(h, counts.data(), V);
+  if (max_id >= V) return bail(fail(h, SGNS_EINVAL, "walk files name vertex %lld >= V = %lld", (long long)max_id, (long long)V));
+  if (V < 2) return bail(fail(h, SGNS_EINVAL, "vocabulary size %lld out of range", (long long)V));
+  // vertex_cn (path.hpp:98) on the device, then the host vocabulary sort
+  std::vector<int32_t> counts((size_t)V, 0);
+  if ((e = cudaMalloc(&d_cnt, sizeof(int32_t) * (size_t)V)) != cudaSuccess ||
+      (e = launch_vertex_count(d_tok, n, d_cnt, V, h->num_sms, h->stream)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(counts.data(), d_cnt, sizeof(int32_t) * (size_t)V, cudaMemcpyDeviceToHost, h->stream)) !=
+          cudaSuccess ||
+      (e = cudaStreamSynchronize(h->stream)) != cudaSuccess)
+    return bail(fail(h, SGNS_ECUDA, "vertex counts: %s", cudaGetErrorString(e)));
+  dfree(d_cnt);
+  st = sgns_set_vocab(h, counts.data(), V);
+  if (st) return bail(st);
+  // the parsed ids become the handle's corpus ids (no host round trip)
+  dfree(h->d_ids);
+  dfree(h->d_corpus);
+  h->d_ids = d_tok;
+  d_tok = nullptr;
+  h->corpus_cap = 0;
+  if ((e = cudaMalloc(&h->d_corpus, sizeof(int32_t) * (size_t)std::max<int64_t>(n, 1))) != cudaSuccess)
+    return bail(fail(h, SGNS_ENOMEM, "corpus of %lld tokens: %s", (long long)n, cudaGetErrorString(e)));
+  h->corpus_cap = n;
+  cleanup();
+  st = map_uploaded_corpus(h, n);
   if (st) return st;
-  return sgns_train_corpus(h, tokens.data(), (int64_t)tokens.size());
+  return sgns_train(h);
 }
 
 sgns_status sgns_minibatch_update(int32_t d, int32_t n, const int32_t* in_count, const int32_t* in_first,

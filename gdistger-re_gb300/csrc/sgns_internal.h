@@ -175,6 +175,15 @@ cudaError_t launch_minibatch(int d, int n, int imax, int omax, const int32_t* in
                              float* d_out, const float* exp_table, int64_t* offsets, int32_t* status,
                              cudaStream_t s);
 // host helpers shared by the translation units (sgns_host.cpp)
+// walk-file text -> corpus (dsgl_ingest.cu); scratch of ingest_scratch_bytes(n) bytes
+size_t ingest_scratch_bytes(int64_t n);
+cudaError_t launch_ingest_count(const uint8_t* bytes, int64_t n, void* scratch, unsigned long long* n_out,
+                                long long* err_pos, cudaStream_t s);
+cudaError_t launch_ingest_emit(const uint8_t* bytes, int64_t n, void* scratch, int32_t* tokens, long long* err_pos,
+                               long long* max_id, cudaStream_t s);
+cudaError_t launch_vertex_count(const int32_t* tokens, int64_t n, int32_t* counts, int64_t V, int num_sms,
+                                cudaStream_t s);
+
 void host_exp_table(float* t /* kExpTableSize + 1 */);
 int report_error(int status, const char* fmt, ...);  // sets sgns_last_error(NULL); returns status
 

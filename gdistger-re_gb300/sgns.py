@@ -90,6 +90,7 @@ def lib():
         L.sgns_save_text.argtypes = [vp, ctypes.c_char_p]
         L.sgns_minibatch_update.argtypes = [i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
         L.sgns_minibatch_update_noalloc.argtypes = [i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+        L.sgns_parse_walks.argtypes = [vp, i64, vp, i64, ctypes.POINTER(i64), ctypes.POINTER(i64), vp]
         L.sgns_loss_adjoint.argtypes = [i32, i32, i64, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp,
                                         ctypes.POINTER(i64), vp, vp, ctypes.POINTER(i64), vp]
         for name in header_functions():  # every declared entry point must be exported
@@ -235,6 +236,27 @@ def minibatch_update_noalloc(d, in_count, in_first, out_count, out_meta, alpha, 
                                                out_meta.data_ptr(), alpha.data_ptr(), in_rows.data_ptr(),
                                                out_rows.data_ptr(), d_in.data_ptr(), d_out.data_ptr(),
                                                ctypes.c_void_p(stream)))
+
+
+def parse_walks(text, tokens=None, stream=0):
+    """sgns_parse_walks on a uint8 device tensor; tokens: int32 device tensor (None: count
+    only).  Returns (n_tokens, max_id)."""
+    n_tok, mx = ctypes.c_int64(), ctypes.c_int64()
+    cap = int(tokens.numel()) if tokens is not None else 0
+    _check(lib().sgns_parse_walks(text.data_ptr() if text.numel() else None, int(text.numel()),
+                                  tokens.data_ptr() if tokens is not None else None, cap, ctypes.byref(n_tok),
+                                  ctypes.byref(mx), ctypes.c_void_p(stream)))
+    return n_tok.value, mx.value
+
+
+def parse_walks_count(text, stream=0):
+    """Number of tokens the walk text yields (the capacity error carries it)."""
+    n_tok, mx = ctypes.c_int64(), ctypes.c_int64()
+    st = lib().sgns_parse_walks(text.data_ptr() if text.numel() else None, int(text.numel()), None, 0,
+                                ctypes.byref(n_tok), ctypes.byref(mx), ctypes.c_void_p(stream))
+    if st not in (OK, EINVAL) or (st == EINVAL and n_tok.value == 0):
+        _check(st)
+    return n_tok.value
 
 
 def loss_adjoint(dtype, d, V, in_ptr, in_ids, in_first, out_ptr, out_ids, out_meta, wih, woh, loss,

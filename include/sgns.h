@@ -128,9 +128,22 @@ sgns_status sgns_train(sgns_handle* h);
 /* Upload + train in one call: the reference's dsgl() hot path from host memory. */
 sgns_status sgns_train_corpus(sgns_handle* h, const int32_t* tokens, int64_t n_tokens);
 /* Reads one or more walk files (" %u" per vertex, one walk per line; path.hpp:92,108),
- * counts vertices, builds the vocabulary over max_vertex_id+1 vertices (or V if V > 0),
- * uploads and trains. */
+ * parses them on the GPU (sgns_parse_walks; the end of each file ends its last walk),
+ * counts vertices (vertex_cn, path.hpp:98) on the GPU, builds the vocabulary over
+ * max_vertex_id+1 vertices (or V if V > 0) and trains on the parsed corpus. */
 sgns_status sgns_train_walk_files(sgns_handle* h, const char* const* paths, int32_t n_paths, int64_t V);
+
+/* Kernel-level walk-text parser, replacing the host reader of word2vec.cu:1002-1041
+ * (strtok on " \n\r\t" per line).  bytes: n bytes of walk text in device memory, read as
+ * one file (the end of the buffer ends its last walk).  tokens: device output of cap
+ * entries: vertex ids in text order with -1 after each line that holds at least one id
+ * (the layout of graph->local_corpus, path.hpp:96,110).  *n_tokens: the number of entries
+ * the text yields, also set when cap is too small (then SGNS_EINVAL is returned and
+ * nothing is written); *max_id: the largest id, -1 if none.  A byte other than a digit,
+ * space, tab, CR or LF, or an id above 2^31 - 1, is SGNS_EINVAL naming its offset.
+ * Ordered on stream; returns after the parse has finished.  Uses library scratch memory. */
+sgns_status sgns_parse_walks(const uint8_t* bytes, int64_t n, int32_t* tokens, int64_t cap, int64_t* n_tokens,
+                             int64_t* max_id, void* stream);
 
 sgns_status sgns_get_stats(const sgns_handle* h, sgns_stats* out);
 int64_t sgns_vocab_size(const sgns_handle* h);

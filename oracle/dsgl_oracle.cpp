@@ -781,4 +781,64 @@ int oracle_minibatch(int32_t acc, int32_t d, int32_t I, int32_t first, int32_t O
   return run(0.0);
 }
 
+// Walk text -> corpus tokens.  The reference writes " %u" per vertex and "\n" after each
+// walk (include/path.hpp:92,108) and its reader splits lines on " \n\r\t"
+// (src/word2vec.cu:1002-1041); this restatement reads ids as integers of at most 10 digits
+// (leading zeros included) no larger than 2^31 - 1, emits -1 after every line that holds an
+// id, and treats the end of the buffer as a final newline.  Returns 0, 1 (a byte other than
+// a digit or separator: *err_pos = its smallest offset; checked before ids), 2 (an id too
+// long or too large: *err_pos = offset of its last digit) or 3 (more than cap tokens;
+// *n_out still says how many).
+int32_t oracle_parse_walks(const uint8_t* b, int64_t n, int32_t* out, int64_t cap, int64_t* n_out,
+                           int64_t* max_id, int64_t* err_pos) {
+  *n_out = 0;
+  *max_id = -1;
+  *err_pos = -1;
+  for (int64_t i = 0; i < n; i++) {
+    const uint8_t c = b[i];
+    if (!((c >= '0' && c <= '9') || c == ' ' || c == '\t' || c == '\r' || c == '\n')) {
+      *err_pos = i;
+      return 1;
+    }
+  }
+  int64_t cnt = 0, val = 0;
+  int nd = 0;
+  bool line_has_ids = false;
+  int32_t code = 0;
+  for (int64_t i = 0; i <= n; i++) {
+    const uint8_t c = i < n ? b[i] : (uint8_t)'\n';
+    if (c >= '0' && c <= '9') {
+      val = val * 10 + (c - '0');
+      nd++;
+      if (nd > 11) val = 0;  // already too long; keep val bounded
+      continue;
+    }
+    if (nd > 0) {
+      if (nd > 10 || val > 2147483647LL) {
+        if (code == 0) {
+          code = 2;
+          *err_pos = i - 1;
+        }
+        val = 0;
+      }
+      if (cnt < cap) out[cnt] = (int32_t)val;
+      cnt++;
+      if (val > *max_id) *max_id = val;
+      line_has_ids = true;
+      nd = 0;
+      val = 0;
+    }
+    if (c == '\n') {
+      if (line_has_ids) {
+        if (cnt < cap) out[cnt] = -1;
+        cnt++;
+      }
+      line_has_ids = false;
+    }
+  }
+  *n_out = cnt;
+  if (code) return code;
+  return cnt > cap ? 3 : 0;
+}
+
 }  // extern "C"

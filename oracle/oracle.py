@@ -55,6 +55,9 @@ def lib():
         L.oracle_lcg_next.argtypes = [ctypes.c_uint64]
         L.oracle_lcg_next.restype = ctypes.c_uint64
         L.oracle_minibatch.argtypes = [i32, i32, i32, i32, i32, vp, ctypes.c_float, vp, vp, vp, vp]
+        L.oracle_parse_walks.argtypes = [vp, i64, vp, i64, ctypes.POINTER(i64), ctypes.POINTER(i64),
+                                         ctypes.POINTER(i64)]
+        L.oracle_parse_walks.restype = i32
         _lib = L
     return _lib
 
@@ -90,6 +93,19 @@ def unigram_table(cn_sorted, table_size, threads):
     t = np.zeros(table_size, np.int32)
     lib().oracle_build_unigram_table(_p(cn_sorted), len(cn_sorted), table_size, threads, _p(t))
     return t
+
+
+def parse_walks(text):
+    """Walk text (bytes) -> (code, tokens int32, max_id, err_pos); code 0 ok, 1 bad byte,
+    2 id too long or too large."""
+    b = np.frombuffer(bytes(text), dtype=np.uint8)
+    n_out, mx, err = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+    code = lib().oracle_parse_walks(_p(b) if len(b) else None, len(b), None, 0, ctypes.byref(n_out),
+                                    ctypes.byref(mx), ctypes.byref(err))
+    out = np.zeros(max(n_out.value, 1), np.int32)
+    code = lib().oracle_parse_walks(_p(b) if len(b) else None, len(b), _p(out), len(out), ctypes.byref(n_out),
+                                    ctypes.byref(mx), ctypes.byref(err))
+    return code, out[:n_out.value], mx.value, err.value
 
 
 def exp_table():
