@@ -440,6 +440,75 @@ def run_sweep(args):
                       "walks": "1/vertex, uniform lengths 5-200", "tokens": int(len(c)), "rows": rows}), flush=True)
 
 
+def format_walk_text(corpus):
+    """Corpus tokens (int32 device tensor, -1 after each walk) -> the reference's walk text
+    (" %u" per vertex, "\n" after each walk) as a uint8 device tensor."""
+    import torch
+
+    v = corpus.long()
+    is_id = v >= 0
+    nd = torch.ones_like(v)
+    for k in range(1, 10):
+        nd += (v >= 10 ** k).long()
+    ln = torch.where(is_id, nd + 1, torch.ones_like(v))
+    end = torch.cumsum(ln, 0)
+    text = torch.full((int(end[-1]),), ord(" "), dtype=torch.uint8, device=corpus.device)
+    text[(end - 1)[~is_id]] = ord("\n")
+    rest = v.clamp(min=0)
+    for k in range(10):
+        m = is_id & (nd > k)
+        text[(end - 1 - k)[m]] = (48 + rest % 10)[m].to(torch.uint8)
+        rest = rest // 10
+    return text
+
+
+def run_ingest(args):
+    """Walk-text parse on the GPU (sgns_parse_walks) on the workload's corpus as text, HBM
+    roofline, and the host restatement of the reference reader on a sample."""
+    import torch
+    import sgns
+    import oracle
+
+    wl = WORKLOADS[args.workload]
+    dev = torch.device("cuda", 0)
+    corpus, _, _, edges, gen_s = make_corpus(wl, 0, dev)
+    text = format_walk_text(corpus)
+    n_text, n_tok = int(text.numel()), int(corpus.numel())
+    tok = torch.empty(n_tok, dtype=torch.int32, device=dev)
+    for _ in range(args.warmup):
+        sgns.parse_walks(text, tok)
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(args.steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        n_out, mx = sgns.parse_walks(text, tok)
+        b.record()
+        torch.cuda.synchronize()
+        ms.append(a.elapsed_time(b))
+    assert n_out == n_tok and bool(torch.equal(tok, corpus)), "parse does not round-trip the corpus"
+    pk = peaks()
+    peak = pk["hbm_gbs"] if pk else 6800.0
+    alg = n_text + 4 * n_tok  # read the text once, write the tokens once
+    t = float(np.median(ms)) / 1e3
+    # host restatement of the reader (single thread), on the first ~256 MB of the text
+    cut = min(n_text, 256 << 20)
+    sample = text[:cut].cpu().numpy().tobytes()
+    t0 = time.time()
+    code, cpu_tok, _, _ = oracle.parse_walks(sample)
+    cpu_s = time.time() - t0
+    line = {"mode": "ingest", "workload": args.workload, "text_bytes": n_text, "tokens": n_tok,
+            "parse_ms": 1e3 * t, "text_GB_per_s": n_text / t / 1e9, "tokens_per_s": n_tok / t,
+            "roofline": {"bound": "hbm", "achieved": alg / t / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": alg / t / 1e9 / peak, "algorithmic_bytes": alg,
+                         "peak_source": "measured" if pk else "fallback"},
+            "cpu_baseline": {"value": cut / cpu_s / 1e9, "unit": "text GB/s", "cores": 1, "kind": "port",
+                             "sample": "first %d bytes of the same text, oracle restatement of the reference "
+                                       "reader (word2vec.cu:1002-1041 separators)" % cut},
+            "steps": args.steps, "warmup": args.warmup}
+    print(json.dumps(line), flush=True)
+
+
 def run_adjoint(args):
     """Forward + hand-written adjoint on reference-shaped minibatches over a 4M-vertex
     Chung-Lu graph, bf16 tables with fp32 accumulation; row-gradient GB/s."""
@@ -501,6 +570,7 @@ def main():
     ap.add_argument("--mb-error", action="store_true", help="bf16 per-minibatch error against fp64")
     ap.add_argument("--sweep", action="store_true", help="d x K x storage sweep, persistent vs plain")
     ap.add_argument("--adjoint", action="store_true", help="loss + adjoint throughput (row-gradient GB/s)")
+    ap.add_argument("--ingest", action="store_true", help="walk-text parse throughput (text GB/s, HBM roofline)")
     ap.add_argument("--adj-vertices", type=int, default=4_000_000)
     ap.add_argument("--adj-batches", type=int, default=200_000)
     args = ap.parse_args()
@@ -508,7 +578,7 @@ def main():
     if args.impl == "reference":
         return run_reference(args, wl)
     for flag, fn in (("auc", run_auc), ("mb_error", run_minibatch_error), ("sweep", run_sweep),
-                     ("adjoint", run_adjoint)):
+                     ("adjoint", run_adjoint), ("ingest", run_ingest)):
         if getattr(args, flag):
             import torch
 

@@ -7,7 +7,9 @@
 // Train_SGNS_MPI reads.  The buffer is read as one file: position n acts as a final
 // newline, so the last walk ends even without one.
 //
-// Three passes over 8 KB tiles (256 threads x 32 bytes, staged in shared memory):
+// Three passes over 8 KB tiles (256 threads x 32 bytes, staged in shared memory with
+// 16-byte loads; each thread classifies its 32 bytes into digit / newline bit masks with
+// byte-wise compares, so ids and walk ends are found with bit operations):
 //   1. each thread summarises its 32 bytes as a Span (outputs it emits, whether its first
 //      significant byte is a newline whose walk end depends on what precedes it, and the
 //      kind of its last significant byte); a block scan gives the tile's Span;
@@ -51,41 +53,113 @@ __host__ __device__ __forceinline__ Span span_combine(Span a, Span b) {
 __device__ __forceinline__ Span span_identity() { return Span{0ull, 0u, SIG_NONE}; }
 
 __device__ __forceinline__ bool is_digit(uint8_t c) { return c >= '0' && c <= '9'; }
-__device__ __forceinline__ bool is_blank(uint8_t c) { return c == ' ' || c == '\t' || c == '\r'; }
 
 // byte i of the text with a virtual newline at n and blanks after it
 __device__ __forceinline__ uint8_t text_byte(const uint8_t* b, int64_t n, int64_t i) {
   return i < n ? __ldg(b + i) : (i == n ? (uint8_t)'\n' : (uint8_t)' ');
 }
 
-// Stages tile bytes [base - halo, base + kIngTile] (one byte of look-ahead) in shared memory.
-__device__ __forceinline__ void stage_tile(const uint8_t* b, int64_t n, int64_t base, uint8_t* s) {
-  for (int k = threadIdx.x; k < kIngHalo + kIngTile + 1; k += blockDim.x) {
-    const int64_t i = base - kIngHalo + k;
-    s[k] = i < 0 ? (uint8_t)' ' : text_byte(b, n, i);
+constexpr int kStageChunks = (kIngHalo + kIngTile + 16) / 16;  // 16-byte chunks staged per tile
+
+// Stages tile bytes [base - halo, base + kIngTile + 16) in shared memory: 16 bytes per load
+// where the chunk lies inside the text and the text starts on a 16-byte boundary (tiles
+// are 8 KB apart, so every chunk is then aligned), byte by byte otherwise.
+__device__ __forceinline__ void stage_tile(const uint8_t* b, int64_t n, int64_t base, bool aligned, uint8_t* s) {
+  for (int c = threadIdx.x; c < kStageChunks; c += blockDim.x) {
+    const int64_t g = base - kIngHalo + 16 * (int64_t)c;
+    uint4 v;
+    if (aligned && g >= 0 && g + 16 <= n) {
+      v = __ldg(reinterpret_cast<const uint4*>(b + g));
+    } else {
+      uint8_t t[16];
+#pragma unroll
+      for (int k = 0; k < 16; k++) t[k] = g + k < 0 ? (uint8_t)' ' : text_byte(b, n, g + k);
+      v = make_uint4(t[0] | t[1] << 8 | t[2] << 16 | (uint32_t)t[3] << 24, t[4] | t[5] << 8 | t[6] << 16 | (uint32_t)t[7] << 24,
+                     t[8] | t[9] << 8 | t[10] << 16 | (uint32_t)t[11] << 24,
+                     t[12] | t[13] << 8 | t[14] << 16 | (uint32_t)t[15] << 24);
+    }
+    reinterpret_cast<uint4*>(s)[c] = v;
   }
   __syncthreads();
 }
 
-// Span of one thread's 32 bytes; s points at the thread's first byte in shared memory.
-__device__ __forceinline__ Span thread_span(const uint8_t* s, int64_t first, int64_t* bad) {
-  Span sp = span_identity();
-  uint32_t cnt = 0;
-#pragma unroll 4
-  for (int j = 0; j < kIngBytes; j++) {
-    const uint8_t c = s[j];
-    if (is_digit(c)) {
-      if (!is_digit(s[j + 1])) cnt++;
-      sp.last = SIG_DIGIT;
-    } else if (c == '\n') {
-      if (sp.last == SIG_DIGIT) cnt++;
-      else if (sp.last == SIG_NONE) sp.pend = 1;
-      sp.last = SIG_NL;
-    } else if (!is_blank(c)) {
-      if (*bad < 0) *bad = first + j;
+// Byte-class tests on 4 bytes at once (SWAR; no carry crosses a byte): 0x80 in each byte
+// that is NOT a decimal digit, resp. in each NONZERO byte.
+__device__ __forceinline__ uint32_t nondigit80(uint32_t w) {
+  const uint32_t t = w ^ 0x30303030u;  // digits become 0..9
+  return (((t & 0x7F7F7F7Fu) + 0x76767676u) | t) & 0x80808080u;
+}
+__device__ __forceinline__ uint32_t nonzero80(uint32_t x) {
+  return (((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x) & 0x80808080u;
+}
+// one bit per byte from a 0x80-per-byte mask
+__device__ __forceinline__ uint32_t nibble(uint32_t m80) { return (m80 * 0x00204081u) >> 28; }
+
+// Class masks of a thread's 32 bytes (bit j = byte j): digits, newlines and, when
+// kCheck, anything that is not a digit, newline, space, tab or CR.
+struct Masks {
+  uint32_t dig, nl, bad;
+};
+template <bool kCheck>
+__device__ __forceinline__ Masks classify(const uint8_t* s) {
+  const uint4 a = reinterpret_cast<const uint4*>(s)[0], c = reinterpret_cast<const uint4*>(s)[1];
+  const uint32_t w[8] = {a.x, a.y, a.z, a.w, c.x, c.y, c.z, c.w};
+  Masks m{0u, 0u, 0u};
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const uint32_t dg = nondigit80(w[k]) ^ 0x80808080u;
+    const uint32_t nl = nonzero80(w[k] ^ 0x0A0A0A0Au) ^ 0x80808080u;
+    m.dig |= nibble(dg) << (4 * k);
+    m.nl |= nibble(nl) << (4 * k);
+    if (kCheck) {
+      const uint32_t bl = (nonzero80(w[k] ^ 0x20202020u) & nonzero80(w[k] ^ 0x09090909u) &
+                           nonzero80(w[k] ^ 0x0D0D0D0Du)) ^ 0x80808080u;
+      m.bad |= nibble(0x80808080u & ~(dg | nl | bl)) << (4 * k);
     }
   }
-  sp.cnt = cnt;
+  return m;
+}
+
+// Outputs of a thread's 32 bytes as bit masks: ends of ids (last digit) and newlines that
+// end a walk given the kind of significant byte before the span (carry: SIG_*; SIG_NONE
+// leaves the first newline undecided and reported in *pend).
+struct Emits {
+  uint32_t ids, walks;
+};
+__device__ __forceinline__ Emits emits(const Masks& m, bool next_digit, uint32_t carry, uint32_t* pend) {
+  Emits e;
+  e.ids = m.dig & ~((m.dig >> 1) | (next_digit ? 0x80000000u : 0u));
+  e.walks = 0;
+  *pend = 0;
+  const uint32_t sig = m.dig | m.nl;
+  uint32_t nls = m.nl;
+  while (nls) {
+    const int p = __ffs(nls) - 1;
+    nls &= nls - 1;
+    const uint32_t before = sig & ((1u << p) - 1u);
+    if (before) {
+      if ((m.dig >> (31 - __clz(before))) & 1u) e.walks |= 1u << p;
+    } else if (carry == SIG_DIGIT) {
+      e.walks |= 1u << p;
+    } else if (carry == SIG_NONE) {
+      *pend = 1;
+    }
+  }
+  return e;
+}
+
+// Span of one thread's 32 bytes; s points at the thread's first byte in shared memory.
+template <bool kCheck>
+__device__ __forceinline__ Span thread_span(const uint8_t* s, int64_t first, int64_t* bad) {
+  const Masks m = classify<kCheck>(s);
+  if (m.bad) *bad = first + __ffs(m.bad) - 1;
+  uint32_t pend;
+  const Emits e = emits(m, is_digit(s[kIngBytes]), SIG_NONE, &pend);
+  const uint32_t sig = m.dig | m.nl;
+  Span sp;
+  sp.cnt = __popc(e.ids) + __popc(e.walks);
+  sp.pend = pend;
+  sp.last = sig == 0 ? SIG_NONE : (((m.dig >> (31 - __clz(sig))) & 1u) ? SIG_DIGIT : SIG_NL);
   return sp;
 }
 
@@ -122,87 +196,115 @@ __device__ __forceinline__ void record_bad(long long* err, int64_t bad) {
   if (bad >= 0) atomicMin(err, (long long)bad);
 }
 
-__global__ void __launch_bounds__(kIngThreads) ingest_count_kernel(const uint8_t* b, int64_t n, Span* tile_span,
-                                                                  long long* err) {
-  __shared__ uint8_t s[kIngHalo + kIngTile + 1];
+__global__ void __launch_bounds__(kIngThreads) ingest_count_kernel(const uint8_t* b, int64_t n, bool aligned,
+                                                                  Span* tile_span, long long* err) {
+  __shared__ __align__(16) uint8_t s[kIngHalo + kIngTile + 16];
   const int64_t base = (int64_t)blockIdx.x * kIngTile;
-  stage_tile(b, n, base, s);
+  stage_tile(b, n, base, aligned, s);
   const int64_t first = base + (int64_t)threadIdx.x * kIngBytes;
   int64_t bad = -1;
-  const Span v = first <= n ? thread_span(s + kIngHalo + threadIdx.x * kIngBytes, first, &bad) : span_identity();
+  const Span v = first <= n ? thread_span<true>(s + kIngHalo + threadIdx.x * kIngBytes, first, &bad) : span_identity();
   record_bad(err, bad);
   Span total;
   block_exclusive(v, &total);
   if (threadIdx.x == 0) tile_span[blockIdx.x] = total;
 }
 
-// Exclusive scan of the tile Spans by one block; the text starts as if after a newline.
+// Exclusive scan of the tile Spans by one block, 1024 consecutive tiles per round (coalesced
+// reads, block scan, carry to the next round); the text starts as if after a newline.
 // out[t] = prefix of tile t; out[ntiles] = the whole text.
 __global__ void __launch_bounds__(kScanBlock) ingest_scan_kernel(const Span* tile_span, int64_t ntiles, Span* out) {
-  __shared__ Span part[kScanBlock];
-  const int64_t per = (ntiles + kScanBlock - 1) / kScanBlock;
-  const int64_t lo = (int64_t)threadIdx.x * per, hi = lo + per < ntiles ? lo + per : ntiles;
-  Span acc = span_identity();
-  for (int64_t t = lo; t < hi; t++) acc = span_combine(acc, tile_span[t]);
-  part[threadIdx.x] = acc;
-  __syncthreads();
-  if (threadIdx.x == 0) {  // 1024 partials: a short serial pass
-    Span run = Span{0ull, 0u, SIG_NL};
-    for (int k = 0; k < kScanBlock; k++) {
-      const Span p = part[k];
-      part[k] = run;
-      run = span_combine(run, p);
+  __shared__ Span warp_tot[kScanBlock / 32];
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  Span carry = Span{0ull, 0u, SIG_NL};
+  for (int64_t r0 = 0; r0 < ntiles; r0 += kScanBlock) {
+    const int64_t t = r0 + threadIdx.x;
+    const Span v = t < ntiles ? tile_span[t] : span_identity();
+    Span inc = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      Span u;
+      u.cnt = __shfl_up_sync(kFull, inc.cnt, o);
+      u.pend = __shfl_up_sync(kFull, inc.pend, o);
+      u.last = __shfl_up_sync(kFull, inc.last, o);
+      if (lane >= o) inc = span_combine(u, inc);
     }
-    out[ntiles] = run;
+    if (lane == 31) warp_tot[wp] = inc;
+    __syncthreads();
+    if (wp == 0) {  // scan of the 32 warp totals
+      Span w = warp_tot[lane];
+      for (int o = 1; o < 32; o <<= 1) {
+        Span u;
+        u.cnt = __shfl_up_sync(kFull, w.cnt, o);
+        u.pend = __shfl_up_sync(kFull, w.pend, o);
+        u.last = __shfl_up_sync(kFull, w.last, o);
+        if (lane >= o) w = span_combine(u, w);
+      }
+      warp_tot[lane] = w;  // inclusive over warps
+    }
+    __syncthreads();
+    Span before = wp > 0 ? warp_tot[wp - 1] : span_identity();
+    Span ex;
+    ex.cnt = __shfl_up_sync(kFull, inc.cnt, 1);
+    ex.pend = __shfl_up_sync(kFull, inc.pend, 1);
+    ex.last = __shfl_up_sync(kFull, inc.last, 1);
+    if (lane == 0) ex = span_identity();
+    if (t < ntiles) out[t] = span_combine(carry, span_combine(before, ex));
+    carry = span_combine(carry, warp_tot[kScanBlock / 32 - 1]);
+    __syncthreads();
   }
-  __syncthreads();
-  Span run = part[threadIdx.x];
-  for (int64_t t = lo; t < hi; t++) {
-    out[t] = run;
-    run = span_combine(run, tile_span[t]);
-  }
+  if (threadIdx.x == 0) out[ntiles] = carry;
 }
 
-__global__ void __launch_bounds__(kIngThreads) ingest_emit_kernel(const uint8_t* b, int64_t n, const Span* tile_prefix,
+__global__ void __launch_bounds__(kIngThreads) ingest_emit_kernel(const uint8_t* b, int64_t n, bool aligned,
+                                                                 const Span* tile_prefix,
                                                                  int32_t* tokens, long long* err,
                                                                  unsigned long long* max_id /* largest id + 1 */) {
-  __shared__ uint8_t s[kIngHalo + kIngTile + 1];
+  __shared__ __align__(16) uint8_t s[kIngHalo + kIngTile + 16];
   const int64_t base = (int64_t)blockIdx.x * kIngTile;
-  stage_tile(b, n, base, s);
+  stage_tile(b, n, base, aligned, s);
   const int64_t first = base + (int64_t)threadIdx.x * kIngBytes;
   const uint8_t* my = s + kIngHalo + threadIdx.x * kIngBytes;
   int64_t bad = -1;
-  const Span v = first <= n ? thread_span(my, first, &bad) : span_identity();
+  // the count pass has checked every byte; this pass only reads valid text
+  const Span v = first <= n ? thread_span<false>(my, first, &bad) : span_identity();
   Span total;
   const Span ex = span_combine(tile_prefix[blockIdx.x], block_exclusive(v, &total));
   long long mx = -1;
   if (first <= n) {
     unsigned long long pos = ex.cnt;
-    uint32_t last = ex.last;
-    for (int j = 0; j < kIngBytes; j++) {
-      const uint8_t c = my[j];
-      if (is_digit(c)) {
-        if (!is_digit(my[j + 1])) {  // last digit of an id: read it backward
-          long long val = 0, scale = 1;
-          int k = j, nd = 0;
-          while (nd <= 10 && is_digit(my[k])) {
-            val += (long long)(my[k] - '0') * scale;
-            scale *= 10;
-            nd++;
-            k--;
-          }
-          if (nd > 10 || val > 2147483647LL) {
-            if (bad < 0) bad = first + j;
-            val = 0;
-          }
-          tokens[pos++] = (int32_t)val;
-          mx = val > mx ? val : mx;
-        }
-        last = SIG_DIGIT;
-      } else if (c == '\n') {
-        if (last == SIG_DIGIT) tokens[pos++] = -1;
-        last = SIG_NL;
+    const Masks m = classify<false>(my);
+    uint32_t pend;
+    const Emits e = emits(m, is_digit(my[kIngBytes]), ex.last, &pend);
+    uint32_t out = e.ids | e.walks;
+    while (out) {  // outputs in text order
+      const int j = __ffs(out) - 1;
+      out &= out - 1;
+      if ((e.walks >> j) & 1u) {
+        tokens[pos++] = -1;
+        continue;
       }
+      // the id ending at byte j, read backward: its last nine digits in 32 bits, then a
+      // tenth (an eleventh digit, or a ten-digit value above 2^31 - 1, is an error)
+      uint32_t low = 0, scale = 1;
+      int k = j, nd = 0;
+      while (nd < 9 && is_digit(my[k])) {
+        low += (uint32_t)(my[k] - '0') * scale;
+        scale *= 10u;
+        nd++;
+        k--;
+      }
+      uint32_t val = low;
+      if (nd == 9 && is_digit(my[k])) {
+        const uint32_t top = (uint32_t)(my[k] - '0');
+        if (is_digit(my[k - 1]) || top > 2u || (top == 2u && low > 147483647u)) {
+          if (bad < 0) bad = first + j;
+          val = 0;
+        } else {
+          val = top * 1000000000u + low;
+        }
+      }
+      tokens[pos++] = (int32_t)val;
+      mx = (long long)val > mx ? (long long)val : mx;
     }
   }
   record_bad(err, bad);
@@ -242,7 +344,8 @@ cudaError_t launch_ingest_count(const uint8_t* bytes, int64_t n, void* scratch, 
   const long long big = 0x7FFFFFFFFFFFFFFFLL;
   cudaError_t e;
   if ((e = cudaMemcpyAsync(err, &big, sizeof big, cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
-  ingest_count_kernel<<<(unsigned)ntiles, kIngThreads, 0, s>>>(bytes, n, tile_span, err);
+  const bool aligned = (reinterpret_cast<uintptr_t>(bytes) & 15) == 0;
+  ingest_count_kernel<<<(unsigned)ntiles, kIngThreads, 0, s>>>(bytes, n, aligned, tile_span, err);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   ingest_scan_kernel<<<1, kScanBlock, 0, s>>>(tile_span, ntiles, prefix);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -264,7 +367,8 @@ cudaError_t launch_ingest_emit(const uint8_t* bytes, int64_t n, void* scratch, i
   unsigned long long* mx = reinterpret_cast<unsigned long long*>(err + 1);
   cudaError_t e;
   if ((e = cudaMemsetAsync(mx, 0, sizeof *mx, s)) != cudaSuccess) return e;
-  ingest_emit_kernel<<<(unsigned)ntiles, kIngThreads, 0, s>>>(bytes, n, prefix, tokens, err, mx);
+  const bool aligned = (reinterpret_cast<uintptr_t>(bytes) & 15) == 0;
+  ingest_emit_kernel<<<(unsigned)ntiles, kIngThreads, 0, s>>>(bytes, n, aligned, prefix, tokens, err, mx);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   unsigned long long m = 0;
   if ((e = cudaMemcpyAsync(err_pos, err, sizeof *err_pos, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||

@@ -111,6 +111,15 @@ def test_gpu_parse_matches_oracle(sgns_lib, oracle_mod):
         out, gmx = _gpu_parse(text, torch)
         assert np.array_equal(out, ref), (len(text), len(out), len(ref))
         assert gmx == mx
+    # text that does not start on a 16-byte boundary (a view at an odd offset)
+    text = random_text(rng, 3000)
+    _, ref, mx, _ = oracle_mod.parse_walks(text)
+    buf = torch.tensor(np.frombuffer(b"123" + text, np.uint8).copy(), device="cuda")
+    view = buf[3:]
+    assert view.data_ptr() % 16 != 0
+    tok = torch.empty(len(ref), dtype=torch.int32, device="cuda")
+    assert sgns.parse_walks(view, tok) == (len(ref), mx)
+    assert np.array_equal(tok.cpu().numpy(), ref)
 
 
 @pytest.mark.gpu
