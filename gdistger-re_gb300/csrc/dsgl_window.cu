@@ -249,7 +249,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
   };
 
   while (true) {
-    if (word_count - last_wc > 10000) {  // dsgl.hpp:886-897
+    if (__builtin_expect(word_count - last_wc > 10000, 0)) {  // dsgl.hpp:886-897
       const uint64_t diff = word_count - last_wc;
       if (lane == 0) {
         unsigned long long now = atomicAdd(&p.ctr->wca, (unsigned long long)diff) + diff;
@@ -258,6 +258,9 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
       last_wc = word_count;
       __syncwarp();
     }
+    // Rare paths (learning-rate update, walk refill, epoch end, pool change, walk end) are
+    // marked unlikely so the compiler keeps them off the per-step instruction stream.
+    if (__builtin_expect(len[0] == 0 || len[1] == 0, 0))
     for (int walk = 0; walk < 2; walk++) {  // dsgl.hpp:902-1030
       while (len[walk] == 0) {
         if (cur >= end) break;
@@ -268,7 +271,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
         enter_initial(walk, n - 1 < w ? n - 1 : w);
       }
     }
-    if (cur >= end) {  // dsgl.hpp:1031-1050
+    if (__builtin_expect(cur >= end, 0)) {  // dsgl.hpp:1031-1050
       if (lane == 0) atomicAdd(&p.ctr->wca, (unsigned long long)(word_count - last_wc));
       if (--local_iter == 0) break;
       word_count = 0;
@@ -279,7 +282,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
       sr0 = sr1 = 0;
       continue;
     }
-    if (change_neg) {  // dsgl.hpp:1054-1088: the pool is its base state and size
+    if (__builtin_expect(change_neg, 0)) {  // dsgl.hpp:1054-1088: the pool is its base state and size
       pool_base = rng;
       neg_n = len[0] > len[1] ? len[0] : len[1];
       neg_g = neg_count % neg_n;
@@ -299,7 +302,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     neg_g = neg_g + 1 == neg_n ? 0 : neg_g + 1;
     const int g = neg_g;
     NegDraw nd;
-    if (g == pf_g) {
+    if (__builtin_expect(g == pf_g, 1)) {
       nd = pf;
       grp_state = pf_gs;
     } else {
@@ -407,7 +410,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
       const int d4 = d >> 2;
       for (int walk = 0; walk < 2; walk++) {
         const uint64_t ev = S == STORE_BF16 ? __shfl_sync(kFull, sr_key, EV_WALK0 + walk) : 0;
-        if (pos[walk] >= len[walk]) {
+        if (__builtin_expect(pos[walk] >= len[walk], 0)) {
           flush_walk(walk, ev);
           len[walk] = 0;
           train_sen_num++;
