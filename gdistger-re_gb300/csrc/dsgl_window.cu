@@ -114,7 +114,9 @@ __device__ __forceinline__ void store_row_from_smem(void* tab, int64_t row, int 
     RowIO<S>::store4(tab, row, d, q, reinterpret_cast<const float4*>(src)[q], ev);
 }
 
-template <int S, int DCH, int OM>
+// kLoss: also accumulate the SGNS loss (compute_loss); without it no loss code is compiled
+// into the step.
+template <int S, int DCH, int OM, bool kLoss>
 __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
   extern __shared__ __align__(16) float smem[];
   float* exp_s = smem;
@@ -357,7 +359,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     const float alpha = *reinterpret_cast<volatile float*>(&p.ctr->alpha);
     auto in_ptr = [&](int j) -> const float* { return rows + (size_t)in_row[j] * DP; };
     forward_gradient_split8<OM>(I, I0, O, d, in_ptr, out_rows, DP, out_meta, exp_s, alpha, corrP,
-                                p.compute_loss != 0, loss);
+                                kLoss, loss);
     float4 md[OM][DCH];
     auto out_pair = [&](int pp, int q, float4& r0, float4& r1) {
       r0 = reinterpret_cast<const float4*>(out_rows + (size_t)(2 * pp) * DP)[q];
@@ -454,7 +456,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
   }
 
   // worker statistics
-  if (p.compute_loss) {
+  if (kLoss) {
     for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(kFull, loss, o);
   }
   if (lane == 0) {
@@ -463,7 +465,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     atomicAdd(&p.ctr->outputs, n_outs);
     atomicAdd(&p.ctr->row_loads, n_loads);
     atomicAdd(&p.ctr->row_stores, n_stores);
-    if (p.compute_loss) atomicAdd(&p.ctr->loss, (double)loss);
+    if (kLoss) atomicAdd(&p.ctr->loss, (double)loss);
     atomicSub(&p.ctr->active, 1);
   }
 }
@@ -478,21 +480,25 @@ size_t window_smem_bytes(int d, int window, int K, int lmax, int warps_per_cta) 
 template <int S, int DCH, int OM>
 static cudaError_t occupancy_t(int d, int w, int K, int lmax, int wpc, int* ctas) {
   const size_t smem = window_smem_bytes(d, w, K, lmax, wpc);
-  cudaError_t e = cudaFuncSetAttribute(window_engine_kernel<S, DCH, OM>,
+  cudaError_t e = cudaFuncSetAttribute(window_engine_kernel<S, DCH, OM, false>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas, window_engine_kernel<S, DCH, OM>, 32 * wpc, smem);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas, window_engine_kernel<S, DCH, OM, false>, 32 * wpc, smem);
 }
 
-template <int S, int DCH, int OM>
-static cudaError_t launch_t(const TrainParams& p, int wpc, cudaStream_t s) {
+template <int S, int DCH, int OM, bool kLoss>
+static cudaError_t launch_loss_t(const TrainParams& p, int wpc, cudaStream_t s) {
   const size_t smem = window_smem_bytes(p.d, p.window, p.K, p.lmax, wpc);
-  cudaError_t e = cudaFuncSetAttribute(window_engine_kernel<S, DCH, OM>,
+  cudaError_t e = cudaFuncSetAttribute(window_engine_kernel<S, DCH, OM, kLoss>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const int blocks = (p.workers + wpc - 1) / wpc;
-  window_engine_kernel<S, DCH, OM><<<blocks, 32 * wpc, smem, s>>>(p);
+  window_engine_kernel<S, DCH, OM, kLoss><<<blocks, 32 * wpc, smem, s>>>(p);
   return cudaGetLastError();
+}
+template <int S, int DCH, int OM>
+static cudaError_t launch_t(const TrainParams& p, int wpc, cudaStream_t s) {
+  return p.compute_loss ? launch_loss_t<S, DCH, OM, true>(p, wpc, s) : launch_loss_t<S, DCH, OM, false>(p, wpc, s);
 }
 
 // kernel variants: storage x column chunks per lane (d <= 128 or <= 256) x outputs per

@@ -140,6 +140,28 @@ def test_replay_exact_mode_on_the_10k_vertex_case(engine, storage, sgns_lib, ora
     assert np.array_equal(woh.view(np.uint32), owoh.view(np.uint32)), np.abs(woh - owoh).max()
 
 
+@pytest.mark.parametrize("engine", ["plain", "persistent"])
+@pytest.mark.parametrize("storage", ["fp32", "bf16"])
+def test_loss_accumulation_leaves_training_unchanged(engine, storage, sgns_lib):
+    """compute_loss selects a kernel that also sums the SGNS loss; with one worker the
+    tables it trains are bit for bit those of the kernel without it."""
+    cfg, corpus, _ = case("cl_d128")
+    counts = np.bincount(corpus[corpus >= 0], minlength=cfg["V"]).astype(np.int32)
+    out = []
+    for loss in (0, 1):
+        opt = sgns.default_options(size=cfg["d"], window=cfg["window"], negative=cfg["negative"], iter=1,
+                                   sample=cfg["sample"], alpha=cfg["alpha"], engine=engine, storage=storage,
+                                   workers=1, warps_per_cta=1, table_size=1000000, debug=0, compute_loss=loss)
+        with sgns.Trainer(opt) as t:
+            t.set_vocab(counts)
+            st = t.train_corpus(corpus)
+            out.append((t.embeddings(0), t.embeddings(1), st))
+    assert np.array_equal(out[0][0].view(np.uint32), out[1][0].view(np.uint32))
+    assert np.array_equal(out[0][1].view(np.uint32), out[1][1].view(np.uint32))
+    assert out[0][2].loss == 0.0 and np.isfinite(out[1][2].loss) and out[1][2].loss > 0.0
+    assert (out[0][2].steps, out[0][2].pairs) == (out[1][2].steps, out[1][2].pairs)
+
+
 @pytest.mark.parametrize("engine,policy", [("plain", 0), ("persistent", 1)])
 def test_many_workers_follow_the_reference_control_flow(engine, policy, sgns_lib, oracle_mod):
     """Hogwild workers race on table rows, but every worker's control flow (slice,
