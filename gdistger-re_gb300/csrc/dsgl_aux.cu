@@ -27,20 +27,33 @@ __global__ void init_wih_kernel(void* wih, int storage, int64_t n, int32_t d, co
 }
 
 // vertex ids -> sorted rows; -1 separators kept; anything else outside [0, V) flagged
-__global__ void map_corpus_kernel(const int32_t* ids, const int32_t* row_of, int32_t* rows, int64_t n,
-                                  int64_t V, int32_t* bad) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t t = ids[i];
-    if (t == -1) {
-      rows[i] = -1;
-    } else if (t < 0 || (int64_t)t >= V) {
-      rows[i] = -1;
-      atomicExch(bad, 1);
-    } else {
-      rows[i] = row_of[t];
-    }
+__device__ __forceinline__ int32_t map_id(int32_t t, const int32_t* row_of, int64_t V, bool* bad) {
+  if (t == -1) return -1;
+  if (t < 0 || (int64_t)t >= V) {
+    *bad = true;
+    return -1;
   }
+  return __ldg(&row_of[t]);
+}
+// ids may be device memory or pinned host memory mapped into the device's address space
+// (then every id crosses the host link once, read in 16-byte pieces when aligned).
+__global__ void map_corpus_kernel(const int32_t* ids, const int32_t* row_of, int32_t* rows, int64_t n,
+                                  int64_t V, int32_t* bad, bool vec4) {
+  bool b = false;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (vec4) {  // ids and rows 16-byte aligned
+    const int64_t n4 = n >> 2;
+    for (int64_t i = t0; i < n4; i += stride) {
+      const int4 v = reinterpret_cast<const int4*>(ids)[i];
+      reinterpret_cast<int4*>(rows)[i] = make_int4(map_id(v.x, row_of, V, &b), map_id(v.y, row_of, V, &b),
+                                                   map_id(v.z, row_of, V, &b), map_id(v.w, row_of, V, &b));
+    }
+    for (int64_t i = (n4 << 2) + t0; i < n; i += stride) rows[i] = map_id(ids[i], row_of, V, &b);
+  } else {
+    for (int64_t i = t0; i < n; i += stride) rows[i] = map_id(ids[i], row_of, V, &b);
+  }
+  if (b) atomicExch(bad, 1);
 }
 
 // ---- explicit-row minibatch update (the step arithmetic of both trainers) ----------
@@ -103,15 +116,22 @@ __global__ void __launch_bounds__(32) minibatch_kernel(int d, int imax, int omax
     }
 }
 
-// each walk start scans forward to its separator (at most kMaxSentence tokens)
+// each walk start scans forward to its separator (at most kMaxSentence tokens); one
+// atomic per warp
 __global__ void max_walk_kernel(const int32_t* rows, int64_t n, int32_t* out) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
+  int best = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     if (rows[i] == -1 || (i > 0 && rows[i - 1] != -1)) continue;
     int len = 0;
     while (i + len < n && rows[i + len] != -1 && len < kMaxSentence) len++;
-    atomicMax(out, len);
+    best = len > best ? len : best;
   }
+  for (int o = 16; o > 0; o >>= 1) {
+    const int t = __shfl_xor_sync(kFull, best, o);
+    best = t > best ? t : best;
+  }
+  if ((threadIdx.x & 31) == 0 && best > 0) atomicMax(out, best);
 }
 
 __global__ void prefix_offsets_kernel(const int32_t* cnt_a, const int32_t* cnt_b, int n, int64_t* off_a,
@@ -142,7 +162,8 @@ cudaError_t launch_map_corpus(const int32_t* ids, const int32_t* row_of, int32_t
   if (n == 0) return cudaSuccess;
   int64_t blocks = (n + 255) / 256;
   if (blocks > 152 * 32) blocks = 152 * 32;
-  map_corpus_kernel<<<(unsigned)blocks, 256, 0, s>>>(ids, row_of, rows, n, V, bad);
+  const bool vec4 = ((reinterpret_cast<uintptr_t>(ids) | reinterpret_cast<uintptr_t>(rows)) & 15) == 0;
+  map_corpus_kernel<<<(unsigned)blocks, 256, 0, s>>>(ids, row_of, rows, n, V, bad, vec4);
   return cudaGetLastError();
 }
 

@@ -660,12 +660,13 @@ sgns_status sgns_reset_model(sgns_handle* h) {
   return SGNS_OK;
 }
 
-// Maps the n ids in h->d_ids to sorted rows (validating them), finds the longest walk.
-sgns_status map_uploaded_corpus(sgns_handle* h, int64_t n) {
+// Maps n ids (device memory, or pinned host memory mapped for this device) to sorted rows
+// (validating them), finds the longest walk.
+sgns_status map_uploaded_corpus(sgns_handle* h, const int32_t* ids, int64_t n) {
   h->n_tokens = n;
   CU(h, cudaMemsetAsync(h->d_flags, 0, 4 * sizeof(int32_t), h->stream));
   if (n > 0) {
-    CU(h, launch_map_corpus(h->d_ids, h->d_row_of, h->d_corpus, n, h->V, h->d_flags, h->stream));
+    CU(h, launch_map_corpus(ids, h->d_row_of, h->d_corpus, n, h->V, h->d_flags, h->stream));
     CU(h, launch_max_walk(h->d_corpus, n, h->d_flags + 1, h->stream));
   }
   CU(h, cudaMemcpyAsync(h->h_flags, h->d_flags, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
@@ -699,8 +700,15 @@ sgns_status sgns_upload_corpus(sgns_handle* h, const int32_t* tokens, int64_t n)
   CU(h, cudaSetDevice(h->opt.device));
   sgns_status st = ensure_corpus_capacity(h, n);
   if (st) return st;
+  // Pinned host memory mapped into this device's address space is read in place by the
+  // mapping kernel (the ids cross the host link once); anything else is copied first.
+  cudaPointerAttributes a{};
+  const bool mapped = n > 0 && cudaPointerGetAttributes(&a, tokens) == cudaSuccess &&
+                      a.type == cudaMemoryTypeHost && a.devicePointer != nullptr && a.device == h->opt.device;
+  cudaGetLastError();  // a failed attribute query leaves no error behind
+  if (mapped) return map_uploaded_corpus(h, static_cast<const int32_t*>(a.devicePointer), n);
   if (n > 0) CU(h, cudaMemcpyAsync(h->d_ids, tokens, sizeof(int32_t) * n, cudaMemcpyHostToDevice, h->stream));
-  return map_uploaded_corpus(h, n);
+  return map_uploaded_corpus(h, h->d_ids, n);
 }
 
 sgns_status sgns_train(sgns_handle* h) {
@@ -1013,7 +1021,7 @@ sgns_status sgns_train_walk_files(sgns_handle* h, const char* const* paths, int3
     return bail(fail(h, SGNS_ENOMEM, "corpus of %lld tokens: %s", (long long)n, cudaGetErrorString(e)));
   h->corpus_cap = n;
   cleanup();
-  st = map_uploaded_corpus(h, n);
+  st = map_uploaded_corpus(h, h->d_ids, n);
   if (st) return st;
   return sgns_train(h);
 }

@@ -162,6 +162,41 @@ def test_loss_accumulation_leaves_training_unchanged(engine, storage, sgns_lib):
     assert (out[0][2].steps, out[0][2].pairs) == (out[1][2].steps, out[1][2].pairs)
 
 
+def test_pinned_host_corpus_is_read_in_place(sgns_lib):
+    """A corpus in pinned host memory is mapped by the kernel without a staging copy; the
+    model equals the one trained from pageable memory, and bad ids are still rejected."""
+    import torch
+
+    cfg, corpus, _ = case("cl_d128")
+    counts = np.bincount(corpus[corpus >= 0], minlength=cfg["V"]).astype(np.int32)
+    pinned = torch.empty(len(corpus) + 3, dtype=torch.int32, pin_memory=True)
+    out = []
+    for src in ("pageable", "pinned", "pinned+4"):
+        opt = sgns.default_options(size=cfg["d"], window=cfg["window"], negative=cfg["negative"], iter=1,
+                                   sample=cfg["sample"], alpha=cfg["alpha"], engine="persistent", storage="bf16",
+                                   mode="exact", table_size=1000000, debug=0)
+        with sgns.Trainer(opt) as t:
+            t.set_vocab(counts)
+            if src == "pageable":
+                st = t.train_corpus(corpus)
+            else:
+                off = 0 if src == "pinned" else 1  # 4 bytes in: not 16-byte aligned
+                pinned[off:off + len(corpus)].copy_(torch.from_numpy(corpus))
+                st = t.train_corpus_ptr(pinned.data_ptr() + 4 * off, len(corpus))
+            out.append((t.embeddings(0), st.pairs))
+    for w, pairs in out[1:]:
+        assert pairs == out[0][1] and np.array_equal(w.view(np.uint32), out[0][0].view(np.uint32))
+    bad = corpus.copy()
+    bad[17] = cfg["V"] + 5
+    pinned[:len(bad)].copy_(torch.from_numpy(bad))
+    with sgns.Trainer(size=cfg["d"], window=cfg["window"], negative=cfg["negative"], table_size=1000000,
+                      debug=0) as t:
+        t.set_vocab(counts)
+        with pytest.raises(sgns.SgnsError) as e:
+            t.train_corpus_ptr(pinned.data_ptr(), len(bad))
+        assert e.value.status == sgns.EINVAL
+
+
 @pytest.mark.parametrize("engine,policy", [("plain", 0), ("persistent", 1)])
 def test_many_workers_follow_the_reference_control_flow(engine, policy, sgns_lib, oracle_mod):
     """Hogwild workers race on table rows, but every worker's control flow (slice,
