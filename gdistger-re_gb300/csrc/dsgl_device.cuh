@@ -479,8 +479,11 @@ __device__ __forceinline__ void backward(int I, int O, int d, InPtr in_ptr, OutP
   for (int i = 0; i < OM; i++)
 #pragma unroll
     for (int t = 0; t < DCH; t++) mlo[i][t] = mhi[i][t] = make_float2(0.f, 0.f);
+  // the next input's row address is fetched one iteration ahead, off the dependency chain
+  const float4* x_next = I > 0 ? reinterpret_cast<const float4*>(in_ptr(0)) : nullptr;
   for (int j = 0; j < I; j++) {
-    const float4* x = reinterpret_cast<const float4*>(in_ptr(j));
+    const float4* x = x_next;
+    x_next = reinterpret_cast<const float4*>(in_ptr(j + 1 < I ? j + 1 : j));
     const float4* cj = reinterpret_cast<const float4*>(corrP + j * SS::CS);
     float2 c[SS::OMP];
 #pragma unroll
