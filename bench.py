@@ -664,6 +664,9 @@ def main():
 
     if not args.skip_extras:
         # e2e through the reference-facing call, host buffers in, statistics out
+        # one untimed call first: the first GPU read of a pinned buffer sets up its host-page
+        # translations (about 0.2 s for 3.2 GB); a caller that reuses the buffer pays it once
+        tr.train_corpus_ptr(corpus_host.data_ptr(), n_tok)
         e2e_t, e2e_pairs, e2e_kernel_ms = [], 0, []
         for it in range(max(1, args.steps)):
             torch.cuda.synchronize()
@@ -678,6 +681,7 @@ def main():
         line["e2e"] = {"value": e2e_pairs_all / e2e_max, "unit": "pairs/s", "h2d_bytes_per_step": 4 * n_tok,
                        "d2h_bytes_per_step": 80,
                        "outside_kernel_ms_per_step": 1e3 * float(np.mean(e2e_t)) - float(np.mean(e2e_kernel_ms))}
+        line["e2e"]["warmup"] = 1
         line["gpu_launches"] = args.steps + 3 * max(1, args.steps)
         tr.close()
         # plain fp32 engine (reference buffer policy, one launch per step) on a 1/8 slice
