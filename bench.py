@@ -40,7 +40,7 @@ METRIC = "SGNS pairs/sec on 1 GB300 (BF16 batched vs plain FP32, same AUC) + HBM
 # captures (dram__bytes_read.sum + dram__bytes_write.sum) of a whole training launch of
 # each workload at 7 warps/CTA; profiles/window_engine_lj-cl_dram.md gives the command.
 # The small workload's tables fit in L2, so its figure does not scale to the large one.
-NCU_DRAM_BYTES_PER_PAIR = {"lj-cl": 1429.11e9 / 7597249326, "small": 50.27e9 / 675874507}
+NCU_DRAM_BYTES_PER_PAIR = {"lj-cl": 1412.52e9 / 7597249326, "small": 48.00e9 / 675874507}
 
 WORKLOADS = {
     "lj-cl": dict(V=2238731, E=30_000_000, gamma=2.1, walks=10, mean=40, cap=80),
