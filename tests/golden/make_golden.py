@@ -83,7 +83,9 @@ def run_case(c):
     meta = dict(c)
     meta.update(wih_sha256=sha(wih), woh_sha256=sha(woh), table_sha256=sha(table), table_size=int(table.size),
                 table_threads=2, exp_sha256=sha(exp), wih_row0=wih[0].tolist(), woh_row0=woh[0].tolist(),
-                wih_last=wih[-1].tolist())
+                wih_last=wih[-1].tolist(),
+                # the reference's own -eoutput file (my_saveModel, dsgl.hpp:1443-1461)
+                text_sha256=hashlib.sha256(open(pre + ".txt", "rb").read()).hexdigest())
     np.savez_compressed(os.path.join(OUT, c["name"] + ".npz"), corpus=corpus, order=order)
     with open(os.path.join(OUT, c["name"] + ".json"), "w") as f:
         json.dump(meta, f, indent=1)

@@ -96,6 +96,46 @@ def test_plain_fp32_reproduces_reference_outputs(name, sgns_lib):
     assert sha(woh) == meta["woh_sha256"]
 
 
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_text_output_is_the_references(name, sgns_lib, tmp_path):
+    """sgns_save_text after a one-worker plain FP32 run writes the reference's own -eoutput
+    file (my_saveModel, dsgl.hpp:1443-1461) byte for byte."""
+    meta, corpus = golden(name)
+    counts = np.bincount(corpus[corpus >= 0], minlength=meta["V"]).astype(np.int32)
+    opt = sgns.default_options(size=meta["d"], window=meta["window"], negative=meta["negative"], iter=meta["iter"],
+                               sample=meta["sample"], alpha=meta["alpha"], engine="plain", storage="fp32",
+                               mode="exact", threads=2, table_size=meta["table_size"], debug=0)
+    out = str(tmp_path / "emb.txt")
+    with sgns.Trainer(opt) as t:
+        t.set_vocab(counts)
+        t.train_corpus(corpus)
+        t.save_text(out)
+    assert hashlib.sha256(open(out, "rb").read()).hexdigest() == meta["text_sha256"]
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_command_line_trainer_on_walk_files(name, sgns_lib, tmp_path):
+    """The sgns_train command line on the golden corpus written as a walk file (" %u" per
+    vertex, one walk per line) reproduces the reference's embedding file byte for byte."""
+    import subprocess
+    import synth
+
+    meta, corpus = golden(name)
+    if corpus[0] == -1 or np.any((corpus[:-1] == -1) & (corpus[1:] == -1)):
+        pytest.skip("holds an empty walk, which a walk file cannot express")
+    walks = str(tmp_path / "walks.txt")
+    synth.write_walk_file(corpus, walks)
+    out = str(tmp_path / "emb.txt")
+    cli = os.path.join(os.path.dirname(sgns.LIB_PATH), "sgns_train")
+    cmd = [cli, "-train", walks, "-eoutput", out, "-size", str(meta["d"]), "-window", str(meta["window"]),
+           "-negative", str(meta["negative"]), "-iter", str(meta["iter"]), "-sample", repr(meta["sample"]),
+           "-alpha", repr(meta["alpha"]), "-threads", "2", "-debug", "0", "-engine", "plain", "-mode", "exact",
+           "-vertices", str(meta["V"]), "-table-size", str(meta["table_size"])]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    assert hashlib.sha256(open(out, "rb").read()).hexdigest() == meta["text_sha256"]
+
+
 @pytest.mark.parametrize("storage", ["fp32", "bf16"])
 @pytest.mark.parametrize("name", ALL_CASES)
 def test_plain_matches_oracle(name, storage, sgns_lib, oracle_mod):
