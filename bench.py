@@ -227,15 +227,20 @@ def run_reference(args, wl):
 # evaluation modes (not the headline line): link-prediction AUC across engines and the
 # CPU reference, bf16 per-minibatch error against fp64, the shape sweep, the adjoint.
 
-def _train_embedding(sgns, counts, corpus_np, V, engine, storage, device, **kw):
+def _train_embedding(sgns, counts, corpus_np, V, engine, storage, device, pos=None, neg=None, **kw):
+    """Trains one engine; returns (embedding in vertex order, stats, AUC scored on the GPU
+    by sgns_link_scores when pos/neg are given)."""
+    import synth
+
     opt = sgns.default_options(iter=1, storage=storage, engine=engine, device=device, debug=0, **{**TRAIN, **kw})
     with sgns.Trainer(opt) as t:
         t.set_vocab(counts)
         t.upload(corpus_np)
         st = t.train()
+        auc = synth.link_auc_device(t, pos, neg) if pos is not None else None
         emb = np.zeros((V, opt.size), np.float32)
         emb[t.order()] = t.embeddings(0)
-        return emb, st
+        return emb, st, auc
 
 
 def run_auc(args):
@@ -264,8 +269,8 @@ def auc_suite(V, cpu=True):
            "tokens": int(len(c)), "train": {**TRAIN, "iter": 1}}
     for name, eng, sto in (("gpu_plain_fp32", "plain", "fp32"), ("gpu_persistent_fp32", "persistent", "fp32"),
                            ("gpu_persistent_bf16", "persistent", "bf16")):
-        emb, st = _train_embedding(sgns, counts, c, V, eng, sto, 0)
-        out[name] = {"auc": synth.link_auc(emb, pos, neg), "pairs_per_s": st.pairs / st.train_ms * 1e3,
+        emb, st, auc = _train_embedding(sgns, counts, c, V, eng, sto, 0, pos, neg)
+        out[name] = {"auc": auc, "pairs_per_s": st.pairs / st.train_ms * 1e3,
                      "workers": st.workers}
     if cpu:
         cores = os.cpu_count() or 1
@@ -509,6 +514,48 @@ def run_ingest(args):
     print(json.dumps(line), flush=True)
 
 
+def run_eval(args):
+    """Link-prediction scoring throughput (sgns_link_scores): random pairs over an LJ-sized
+    BF16 table, HBM roofline; the oracle's restatement on a host sample."""
+    import torch
+    import sgns
+    import oracle
+
+    V, d, n = WORKLOADS["lj-cl"]["V"], TRAIN["size"], 50_000_000
+    g = torch.Generator(device="cuda").manual_seed(9)
+    table = (torch.randn(V, d, device="cuda", generator=g) * 0.1).to(torch.bfloat16)
+    pairs = torch.randint(0, V, (n, 2), device="cuda", dtype=torch.int32, generator=g)
+    scores = torch.empty(n, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        sgns.link_scores(1, d, table, V, pairs, scores)
+    ms = []
+    for _ in range(args.steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        sgns.link_scores(1, d, table, V, pairs, scores)
+        b.record()
+        torch.cuda.synchronize()
+        ms.append(a.elapsed_time(b))
+    t = float(np.median(ms)) / 1e3
+    alg = n * (2 * d * 2 + 8 + 4)  # two bf16 rows, the pair, the score
+    pk = peaks()
+    peak = pk["hbm_gbs"] if pk else 6800.0
+    m = 1_000_000
+    host_tab = table.view(torch.int16).cpu().numpy().view(np.uint16)
+    hp = pairs[:m].cpu().numpy()
+    t0 = time.time()
+    ref, _ = oracle.link_scores(host_tab, hp)
+    cpu_s = time.time() - t0
+    assert np.array_equal(ref.view(np.uint32), scores[:m].cpu().numpy().view(np.uint32)), "scores differ from the oracle"
+    print(json.dumps({"mode": "eval", "table": "V=%d d=%d bf16" % (V, d), "pairs": n, "ms": 1e3 * t,
+                      "pairs_per_s": n / t,
+                      "roofline": {"bound": "hbm", "achieved": alg / t / 1e9, "peak": peak, "unit": "GB/s",
+                                   "frac": alg / t / 1e9 / peak, "algorithmic_bytes": alg},
+                      "cpu_baseline": {"value": m / cpu_s, "unit": "pairs/s", "cores": 1, "kind": "port",
+                                       "sample": "first %d pairs, oracle restatement (same summation order; "
+                                                 "scores equal bit for bit)" % m}}), flush=True)
+
+
 def run_adjoint(args):
     """Forward + hand-written adjoint on reference-shaped minibatches over a 4M-vertex
     Chung-Lu graph, bf16 tables with fp32 accumulation; row-gradient GB/s."""
@@ -571,6 +618,7 @@ def main():
     ap.add_argument("--sweep", action="store_true", help="d x K x storage sweep, persistent vs plain")
     ap.add_argument("--adjoint", action="store_true", help="loss + adjoint throughput (row-gradient GB/s)")
     ap.add_argument("--ingest", action="store_true", help="walk-text parse throughput (text GB/s, HBM roofline)")
+    ap.add_argument("--eval", action="store_true", help="link-prediction scoring throughput (pairs/s, HBM roofline)")
     ap.add_argument("--adj-vertices", type=int, default=4_000_000)
     ap.add_argument("--adj-batches", type=int, default=200_000)
     args = ap.parse_args()
@@ -578,7 +626,7 @@ def main():
     if args.impl == "reference":
         return run_reference(args, wl)
     for flag, fn in (("auc", run_auc), ("mb_error", run_minibatch_error), ("sweep", run_sweep),
-                     ("adjoint", run_adjoint), ("ingest", run_ingest)):
+                     ("adjoint", run_adjoint), ("ingest", run_ingest), ("eval", run_eval)):
         if getattr(args, flag):
             import torch
 

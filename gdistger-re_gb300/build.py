@@ -16,7 +16,7 @@ ROOT = os.path.dirname(HERE)
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["dsgl_window.cu", "dsgl_plain.cu", "dsgl_aux.cu", "dsgl_adjoint.cu", "dsgl_noalloc.cu",
-              "dsgl_ingest.cu"]
+              "dsgl_ingest.cu", "dsgl_eval.cu"]
 CPP_SOURCES = ["sgns_host.cpp"]
 LIB = os.path.join(OUT, "libsgns.so")
 CLI = os.path.join(OUT, "sgns_train")

@@ -1051,6 +1051,34 @@ sgns_status sgns_minibatch_update(int32_t d, int32_t n, const int32_t* in_count,
   return SGNS_OK;
 }
 
+sgns_status sgns_link_scores(int32_t dtype, int32_t d, const void* table, int64_t V, const int32_t* pairs,
+                             int64_t n, float* scores, void* stream) {
+  if ((dtype != 0 && dtype != 1) || d < 4 || d > kDMax || d % 4 || V < 1 || n < 0 ||
+      (n > 0 && (!table || !pairs || !scores)))
+    return fail(nullptr, SGNS_EINVAL, "bad link-score arguments");
+  if (n == 0) return SGNS_OK;
+  DeviceScratch* ds = device_scratch();
+  if (!ds) return fail(nullptr, SGNS_ECUDA, "no current CUDA device");
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return fail(nullptr, SGNS_ECUDA, "device query failed");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  std::lock_guard<std::mutex> g(ds->mx);
+  sgns_status st = ds->ensure(16);
+  if (st) return st;
+  int32_t* bad = static_cast<int32_t*>(ds->buf);
+  int32_t hb = 0;
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(bad, 0, sizeof(int32_t), s)) != cudaSuccess ||
+      (e = launch_link_scores(dtype == 1 ? STORE_BF16 : STORE_F32, table, d, V, pairs, n, scores, bad, sms, s)) !=
+          cudaSuccess ||
+      (e = cudaMemcpyAsync(&hb, bad, sizeof hb, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    return fail(nullptr, SGNS_ECUDA, "link scores: %s", cudaGetErrorString(e));
+  if (hb) return fail(nullptr, SGNS_EINVAL, "a pair names a row outside [0, %lld)", (long long)V);
+  return SGNS_OK;
+}
+
 sgns_status sgns_loss_adjoint(int32_t dtype, int32_t d, int64_t V, int32_t n, const int32_t* in_ptr,
                               const int32_t* in_ids, const int32_t* in_first, const int32_t* out_ptr,
                               const int32_t* out_ids, const int32_t* out_meta, const void* wih, const void* woh,

@@ -184,6 +184,10 @@ cudaError_t launch_ingest_emit(const uint8_t* bytes, int64_t n, void* scratch, i
 cudaError_t launch_vertex_count(const int32_t* tokens, int64_t n, int32_t* counts, int64_t V, int num_sms,
                                 cudaStream_t s);
 
+// link-prediction scores (dsgl_eval.cu); *bad set to 1 for a pair outside [0, V)
+cudaError_t launch_link_scores(int storage, const void* table, int d, int64_t V, const int32_t* pairs, int64_t n,
+                               float* scores, int32_t* bad, int num_sms, cudaStream_t s);
+
 void host_exp_table(float* t /* kExpTableSize + 1 */);
 int report_error(int status, const char* fmt, ...);  // sets sgns_last_error(NULL); returns status
 

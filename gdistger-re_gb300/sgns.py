@@ -91,6 +91,7 @@ def lib():
         L.sgns_minibatch_update.argtypes = [i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
         L.sgns_minibatch_update_noalloc.argtypes = [i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
         L.sgns_parse_walks.argtypes = [vp, i64, vp, i64, ctypes.POINTER(i64), ctypes.POINTER(i64), vp]
+        L.sgns_link_scores.argtypes = [i32, i32, vp, i64, vp, i64, vp, vp]
         L.sgns_loss_adjoint.argtypes = [i32, i32, i64, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp,
                                         ctypes.POINTER(i64), vp, vp, ctypes.POINTER(i64), vp]
         for name in header_functions():  # every declared entry point must be exported
@@ -257,6 +258,15 @@ def parse_walks_count(text, stream=0):
     if st not in (OK, EINVAL) or (st == EINVAL and n_tok.value == 0):
         _check(st)
     return n_tok.value
+
+
+def link_scores(dtype, d, table, V, pairs, scores, stream=0):
+    """sgns_link_scores: table is a device pointer (int) or tensor of V x d (fp32 or bf16
+    bits), pairs an int32 device tensor of shape [n, 2] (row indices), scores a float32
+    device tensor of n entries."""
+    tp = table if isinstance(table, int) else table.data_ptr()
+    _check(lib().sgns_link_scores(dtype, d, ctypes.c_void_p(tp), V, pairs.data_ptr(), int(pairs.shape[0]),
+                                  scores.data_ptr(), ctypes.c_void_p(stream)))
 
 
 def loss_adjoint(dtype, d, V, in_ptr, in_ids, in_first, out_ptr, out_ids, out_meta, wih, woh, loss,

@@ -299,11 +299,38 @@ def link_auc(emb, pos, neg):
     e = e.cpu()
     sp = (e[pos[0]] * e[pos[1]]).sum(1)
     sn = (e[neg[0]] * e[neg[1]]).sum(1)
+    return auc_from_scores(sp, sn)
+
+
+def link_auc_device(trainer, pos, neg):
+    """The same AUC with the scores computed on the GPU by sgns_link_scores from the
+    trainer's input table (rows in sorted order; vertex ids mapped through its order)."""
+    import sgns
+
+    order = torch.as_tensor(trainer.order().astype(np.int64))
+    row_of = torch.empty_like(order)
+    row_of[order] = torch.arange(order.numel())
+    V, d = order.numel(), trainer.opt.size
+    wih, _ = trainer.device_tables()
+    dtype = 1 if trainer.opt.storage == sgns.STORE_BF16_SR else 0
+    out = []
+    for p in (pos, neg):
+        p = torch.as_tensor(p).long().cpu()
+        pairs = torch.stack([row_of[p[0]], row_of[p[1]]], 1).to(torch.int32).cuda()
+        sc = torch.empty(pairs.shape[0], dtype=torch.float32, device="cuda")
+        sgns.link_scores(dtype, d, wih, V, pairs, sc)
+        out.append(sc)
+    return auc_from_scores(out[0], out[1])
+
+
+def auc_from_scores(sp, sn):
+    """Mann-Whitney AUC of positive scores sp against negative scores sn (ties averaged),
+    in fp64 on the scores' device."""
     scores = torch.cat([sp, sn]).double()
     labels = torch.cat([torch.ones_like(sp), torch.zeros_like(sn)]).double()
     order = torch.argsort(scores)
     ranks = torch.empty_like(scores)
-    ranks[order] = torch.arange(1, scores.numel() + 1, dtype=torch.float64)
+    ranks[order] = torch.arange(1, scores.numel() + 1, dtype=torch.float64, device=scores.device)
     # average ranks of ties
     s_sorted = scores[order]
     uniq, inv, cnt = torch.unique_consecutive(s_sorted, return_inverse=True, return_counts=True)

@@ -189,6 +189,16 @@ sgns_status sgns_minibatch_update_noalloc(int32_t d, int32_t n_batches, const in
                                           const float* in_rows, const float* out_rows, float* d_in,
                                           float* d_out, void* stream);
 
+/* Link-prediction scores: scores[i] = <table[pairs[2i]], table[pairs[2i+1]]> for n pairs of
+ * row indices into a table of V rows (device pointers; the dot-product scoring of the
+ * holdout that src/tools/gtrain.cpp:226-385 writes).  dtype: 0 = fp32 table, 1 = bf16
+ * table; fp32 arithmetic in a fixed order (per lane columns 4l..4l+3 of each 128-column
+ * chunk by fused multiply-adds, then an xor butterfly over the 32 lanes).  A pair naming a
+ * row outside [0, V) scores 0 and makes the call return SGNS_EINVAL.  Ordered on stream;
+ * returns after the scores are written. */
+sgns_status sgns_link_scores(int32_t dtype, int32_t d, const void* table, int64_t V, const int32_t* pairs,
+                             int64_t n, float* scores, void* stream);
+
 /* SGNS loss and its hand-written adjoint for n minibatches that index tables of V
  * rows (device pointers).  Minibatch b has inputs in_ids[in_ptr[b]..in_ptr[b+1]), the
  * first in_first[b] of them labelled by output 0 and the rest by the last output, and

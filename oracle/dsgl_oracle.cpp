@@ -841,4 +841,40 @@ int32_t oracle_parse_walks(const uint8_t* b, int64_t n, int32_t* out, int64_t ca
   return cnt > cap ? 3 : 0;
 }
 
+// Link-prediction score of pair (u, v): <table[u], table[v]> in fp32, in the GPU kernel's
+// fixed order -- lane l (0..31) sums columns 4l..4l+3 of each 128-column chunk with fused
+// multiply-adds, then the lane sums are combined by an xor butterfly (16, 8, 4, 2, 1).
+// dtype 0: fp32 table; 1: bf16 table (raw bits).  Returns 1 if a pair is outside [0, V)
+// (its score is 0), else 0.
+int32_t oracle_link_scores(int32_t dtype, int32_t d, const void* table, int64_t V, const int32_t* pairs, int64_t n,
+                           float* scores) {
+  int32_t bad = 0;
+  auto at = [&](int64_t row, int c) -> float {
+    if (dtype == 1) return bf16_to_f32(static_cast<const uint16_t*>(table)[row * d + c]);
+    return static_cast<const float*>(table)[row * d + c];
+  };
+  for (int64_t i = 0; i < n; i++) {
+    const int32_t u = pairs[2 * i], v = pairs[2 * i + 1];
+    if (u < 0 || v < 0 || u >= V || v >= V) {
+      scores[i] = 0.f;
+      bad = 1;
+      continue;
+    }
+    float lane[32];
+    for (int l = 0; l < 32; l++) {
+      float acc = 0.f;
+      for (int q = l; q < d / 4; q += 32)
+        for (int k = 0; k < 4; k++) acc = fmaf(at(u, 4 * q + k), at(v, 4 * q + k), acc);
+      lane[l] = acc;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      float next[32];
+      for (int l = 0; l < 32; l++) next[l] = lane[l] + lane[l ^ o];
+      for (int l = 0; l < 32; l++) lane[l] = next[l];
+    }
+    scores[i] = lane[0];
+  }
+  return bad;
+}
+
 }  // extern "C"

@@ -58,6 +58,8 @@ def lib():
         L.oracle_parse_walks.argtypes = [vp, i64, vp, i64, ctypes.POINTER(i64), ctypes.POINTER(i64),
                                          ctypes.POINTER(i64)]
         L.oracle_parse_walks.restype = i32
+        L.oracle_link_scores.argtypes = [i32, i32, vp, i64, vp, i64, vp]
+        L.oracle_link_scores.restype = i32
         _lib = L
     return _lib
 
@@ -106,6 +108,21 @@ def parse_walks(text):
     code = lib().oracle_parse_walks(_p(b) if len(b) else None, len(b), _p(out), len(out), ctypes.byref(n_out),
                                     ctypes.byref(mx), ctypes.byref(err))
     return code, out[:n_out.value], mx.value, err.value
+
+
+def link_scores(table, pairs):
+    """table: [V, d] float32, or uint16 bf16 bits; pairs: [n, 2] int32 rows.
+    Returns (scores float32 [n], any pair out of range)."""
+    table = np.ascontiguousarray(table)
+    pairs = np.ascontiguousarray(pairs, dtype=np.int32)
+    dtype = 1 if table.dtype == np.uint16 else 0
+    if dtype == 0:
+        table = table.astype(np.float32, copy=False)
+    V, d = table.shape
+    scores = np.zeros(len(pairs), np.float32)
+    bad = lib().oracle_link_scores(dtype, d, _p(table), V, _p(pairs) if len(pairs) else None, len(pairs),
+                                   _p(scores) if len(pairs) else None)
+    return scores, bool(bad)
 
 
 def exp_table():
