@@ -377,6 +377,111 @@ __device__ __forceinline__ void forward_gradient(int I, int first, int O, int d,
 // as s_m = even_m + odd_m, f = (s_0 + s_1) + (s_2 + s_3) when d % 16 == 0; when not,
 // [0, d) is one range and f = even + odd.  The oracle's window policy uses the same
 // order.  out_rows: normal layout, stride DP.
+// One round over inputs j0..j0+nj-1 with L lanes per input (NQ * L == 4 quarters per
+// input, or kWhole: the whole range, one lane per input).  Lane pairs (L == 2) each hold
+// (s0 + s1) or (s2 + s3) and add the other's with a shuffle (a + b == b + a bit for bit).
+template <int NQ, int L, bool kWhole, int OM, class InPtr>
+__device__ __forceinline__ void forward_round(int j0, int nj, int first, int O, int q4, InPtr in_ptr,
+                                              const float* out_rows, int DP, const int* out_meta,
+                                              const float* exp_table, float alpha, float2* corrP,
+                                              bool want_loss, float& loss) {
+  typedef StepShape<OM> SS;
+  const int lane = lane_id();
+  const int jl = lane / L, sub = lane % L;
+  const int j = j0 + jl;
+  const bool active = jl < nj;
+  const float4* x = reinterpret_cast<const float4*>(in_ptr(active ? j : j0));
+  const int m0 = sub * NQ;
+  float2 f[OM][NQ];
+#pragma unroll
+  for (int i = 0; i < OM; i++)
+#pragma unroll
+    for (int m = 0; m < NQ; m++) f[i][m] = make_float2(0.f, 0.f);
+  for (int k4 = 0; k4 < q4; k4++) {
+    float4 xv[NQ];
+#pragma unroll
+    for (int m = 0; m < NQ; m++) xv[m] = x[(m0 + m) * q4 + k4];
+#pragma unroll
+    for (int i = 0; i < OM; i++) {
+      const float4* orow = reinterpret_cast<const float4*>(out_rows + (size_t)i * DP);
+#pragma unroll
+      for (int m = 0; m < NQ; m++) {
+        const float4 o = orow[(m0 + m) * q4 + k4];
+        f[i][m] = ffma2(make_float2(o.x, o.y), make_float2(xv[m].x, xv[m].y), f[i][m]);
+        f[i][m] = ffma2(make_float2(o.z, o.w), make_float2(xv[m].z, xv[m].w), f[i][m]);
+      }
+    }
+  }
+  float fv[OM];
+#pragma unroll
+  for (int i = 0; i < OM; i++) {
+    if (kWhole) {
+      fv[i] = __fadd_rn(f[i][0].x, f[i][0].y);
+    } else if (NQ == 4) {
+      const float s0 = __fadd_rn(f[i][0].x, f[i][0].y), s1 = __fadd_rn(f[i][1 % NQ].x, f[i][1 % NQ].y);
+      const float s2 = __fadd_rn(f[i][2 % NQ].x, f[i][2 % NQ].y), s3 = __fadd_rn(f[i][3 % NQ].x, f[i][3 % NQ].y);
+      fv[i] = __fadd_rn(__fadd_rn(s0, s1), __fadd_rn(s2, s3));
+    } else {
+      const float a = __fadd_rn(__fadd_rn(f[i][0].x, f[i][0].y), __fadd_rn(f[i][1 % NQ].x, f[i][1 % NQ].y));
+      fv[i] = __fadd_rn(a, __shfl_xor_sync(kFull, a, 1));
+    }
+  }
+  if (active && sub == 0) {
+#pragma unroll
+    for (int i = 0; i < OM; i++) {
+      if (i < O) {
+        const float fi = fv[i];
+        const int label = j < first ? (i == 0) : (i == 1);  // outputs t1, t2, negatives
+        float g;
+        if (fi > (float)kMaxExp) {
+          g = __fmul_rn((float)(label - 1), alpha);
+        } else if (fi < -(float)kMaxExp) {
+          g = __fmul_rn((float)label, alpha);
+        } else {
+          const int idx = __float2int_rz(__fmul_rn(__fadd_rn(fi, (float)kMaxExp), (float)kTableScale));
+          g = __fmul_rn(__fsub_rn((float)label, exp_table[idx]), alpha);
+        }
+        const float gm = __fmul_rn(g, (float)out_meta[i]);
+        corrP[j * SS::CS + i] = make_float2(gm, gm);
+        if (want_loss) {
+          const float z = label ? -fi : fi;
+          loss += (float)out_meta[i] * (fmaxf(z, 0.f) + log1pf(__expf(-fabsf(z))));
+        }
+      }
+    }
+  }
+}
+
+// The split forward with two lanes per input while at most 16 inputs remain (each lane sums
+// two of the four quarters): half the k-loop per lane for those rounds, the same bits.
+template <int OM, class InPtr>
+__device__ __forceinline__ void forward_gradient_two_lanes(int I, int first, int O, int d, InPtr in_ptr,
+                                                        const float* out_rows, int DP, const int* out_meta,
+                                                        const float* exp_table, float alpha, float2* corrP,
+                                                        bool want_loss, float& loss) {
+  if ((d & 15) == 0) {
+    const int q4 = d >> 4;
+    for (int j0 = 0; j0 < I;) {
+      const int rem = I - j0;
+      if (rem <= 16) {
+        forward_round<2, 2, false, OM>(j0, rem, first, O, q4, in_ptr, out_rows, DP, out_meta, exp_table, alpha,
+                                       corrP, want_loss, loss);
+        j0 += rem;
+      } else {
+        const int nj = rem < 32 ? rem : 32;
+        forward_round<4, 1, false, OM>(j0, nj, first, O, q4, in_ptr, out_rows, DP, out_meta, exp_table, alpha,
+                                       corrP, want_loss, loss);
+        j0 += nj;
+      }
+    }
+  } else {
+    for (int j0 = 0; j0 < I; j0 += 32)
+      forward_round<1, 1, true, OM>(j0, I - j0 < 32 ? I - j0 : 32, first, O, d >> 2, in_ptr, out_rows, DP,
+                                    out_meta, exp_table, alpha, corrP, want_loss, loss);
+  }
+  __syncwarp();
+}
+
 template <int OM, class InPtr>
 __device__ __forceinline__ void forward_gradient_split8(int I, int first, int O, int d, InPtr in_ptr,
                                                         const float* out_rows, int DP, const int* out_meta,

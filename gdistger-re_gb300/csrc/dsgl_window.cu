@@ -358,8 +358,13 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     __syncwarp();
     const float alpha = *reinterpret_cast<volatile float*>(&p.ctr->alpha);
     auto in_ptr = [&](int j) -> const float* { return rows + (size_t)in_row[j] * DP; };
-    forward_gradient_split8<OM>(I, I0, O, d, in_ptr, out_rows, DP, out_meta, exp_s, alpha, corrP,
-                                kLoss, loss);
+    // two lanes per input for small rounds pays for fp32 tables with d <= 128, K <= 5 (the
+    // other variants have no registers to spare)
+    if (S == STORE_F32 && DCH == 1 && OM == 7)
+      forward_gradient_two_lanes<OM>(I, I0, O, d, in_ptr, out_rows, DP, out_meta, exp_s, alpha, corrP, kLoss, loss);
+    else
+      forward_gradient_split8<OM>(I, I0, O, d, in_ptr, out_rows, DP, out_meta, exp_s, alpha, corrP,
+                                  kLoss, loss);
     float4 md[OM][DCH];
     auto out_pair = [&](int pp, int q, float4& r0, float4& r1) {
       r0 = reinterpret_cast<const float4*>(out_rows + (size_t)(2 * pp) * DP)[q];
