@@ -72,6 +72,46 @@ def test_create_without_gpu_fails_loudly(sgns_lib):
     assert e.value.status == sgns.ECUDA
 
 
+def test_kernel_level_entry_points_check_arguments_first(sgns_lib):
+    """Bad arguments are rejected with SGNS_EINVAL before any device is touched."""
+    import ctypes
+
+    L = sgns.lib()
+    n_tok, mx = ctypes.c_int64(), ctypes.c_int64()
+    # walk-text parse: null text of nonzero size, negative size, capacity without a buffer
+    assert L.sgns_parse_walks(None, 5, None, 0, ctypes.byref(n_tok), ctypes.byref(mx), None) == sgns.EINVAL
+    assert L.sgns_parse_walks(None, -1, None, 0, ctypes.byref(n_tok), ctypes.byref(mx), None) == sgns.EINVAL
+    fake = ctypes.c_void_p(16)  # never dereferenced: the call fails on the missing output
+    assert L.sgns_parse_walks(fake, 4, None, 8, ctypes.byref(n_tok), ctypes.byref(mx), None) == sgns.EINVAL
+    # link scores: unknown dtype, d not a multiple of 4, d too large, missing buffers
+    for args in ((2, 8, fake, 10, fake, 1, fake), (0, 6, fake, 10, fake, 1, fake),
+                 (0, 512, fake, 10, fake, 1, fake), (0, 8, None, 10, fake, 1, fake)):
+        assert L.sgns_link_scores(*args, None) == sgns.EINVAL
+    assert b"link-score" in L.sgns_last_error(None)
+    assert L.sgns_link_scores(0, 8, fake, 10, fake, 0, fake, None) == sgns.OK  # nothing to do
+
+
+def test_walk_text_formatter_writes_the_reference_format():
+    """bench.format_walk_text (the text the ingest benchmark parses) is the reference's
+    walk format, byte for byte as synth.write_walk_file writes it."""
+    import os
+    import sys
+    import tempfile
+    import torch
+
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    import synth
+
+    rng = np.random.default_rng(8)
+    walks = [rng.integers(0, 2**31 - 1 if k % 5 == 0 else 100000, size=rng.integers(1, 30)) for k in range(200)]
+    corpus = np.concatenate([np.append(w, -1) for w in walks]).astype(np.int32)
+    text = bench.format_walk_text(torch.from_numpy(corpus)).numpy().tobytes()
+    path = os.path.join(tempfile.mkdtemp(), "w.txt")
+    synth.write_walk_file(corpus, path)
+    assert text == open(path, "rb").read()
+
+
 # ---- arithmetic the kernels rely on, restated exactly in Python ---------------------
 def gm_magic(d):
     l = 0
