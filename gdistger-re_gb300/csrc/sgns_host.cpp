@@ -21,10 +21,18 @@
 #include <thread>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>  // header-only; ranges are free unless a profiler is attached
+
 #include "sgns.h"
 #include "sgns_internal.h"
 
 using namespace sgns;
+
+// NVTX range for the duration of a scope (library phases in a profiler timeline)
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
 
 struct sgns_handle {
   sgns_options opt{};
@@ -588,6 +596,7 @@ const char* sgns_last_error(const sgns_handle* h) {
 }
 
 sgns_status sgns_set_vocab(sgns_handle* h, const int32_t* counts, int64_t V) {
+  NvtxRange r_("sgns_set_vocab");
   if (!h || !counts) return fail(h, SGNS_EINVAL, "null argument");
   if (V < 2 || V > (int64_t)INT32_MAX) return fail(h, SGNS_EINVAL, "vocabulary size %lld out of range", (long long)V);
   CU(h, cudaSetDevice(h->opt.device));
@@ -695,6 +704,7 @@ sgns_status ensure_corpus_capacity(sgns_handle* h, int64_t n) {
 }
 
 sgns_status sgns_upload_corpus(sgns_handle* h, const int32_t* tokens, int64_t n) {
+  NvtxRange r_("sgns_upload_corpus");
   if (!h || (!tokens && n > 0) || n < 0) return fail(h, SGNS_EINVAL, "bad corpus arguments");
   if (!h->wih) return fail(h, SGNS_ESTATE, "sgns_set_vocab has not been called");
   CU(h, cudaSetDevice(h->opt.device));
@@ -712,6 +722,7 @@ sgns_status sgns_upload_corpus(sgns_handle* h, const int32_t* tokens, int64_t n)
 }
 
 sgns_status sgns_train(sgns_handle* h) {
+  NvtxRange r_("sgns_train");
   if (!h) return fail(h, SGNS_EINVAL, "null handle");
   if (!h->wih) return fail(h, SGNS_ESTATE, "sgns_set_vocab has not been called");
   CU(h, cudaSetDevice(h->opt.device));
@@ -823,6 +834,7 @@ sgns_status sgns_device_tables(sgns_handle* h, void** wih, void** woh) {
 }
 
 sgns_status sgns_save_text(sgns_handle* h, const char* path) {
+  NvtxRange r_("sgns_save_text");
   if (!h || !path) return fail(h, SGNS_EINVAL, "bad arguments");
   if (!h->wih) return fail(h, SGNS_ESTATE, "sgns_set_vocab has not been called");
   const int64_t V = h->V;
@@ -903,12 +915,14 @@ sgns_status parse_walks(sgns_handle* h, const uint8_t* bytes, int64_t n, int32_t
 
 sgns_status sgns_parse_walks(const uint8_t* bytes, int64_t n, int32_t* tokens, int64_t cap, int64_t* n_tokens,
                              int64_t* max_id, void* stream) {
+  NvtxRange r_("sgns_parse_walks");
   if ((!bytes && n > 0) || n < 0 || cap < 0 || (cap > 0 && !tokens) || !n_tokens || !max_id)
     return fail(nullptr, SGNS_EINVAL, "bad walk-parse arguments");
   return parse_walks(nullptr, bytes, n, tokens, cap, n_tokens, max_id, static_cast<cudaStream_t>(stream));
 }
 
 sgns_status sgns_train_walk_files(sgns_handle* h, const char* const* paths, int32_t n_paths, int64_t V) {
+  NvtxRange r_("sgns_train_walk_files");
   if (!h || !paths || n_paths <= 0) return fail(h, SGNS_EINVAL, "bad arguments");
   CU(h, cudaSetDevice(h->opt.device));
   // total text: each file followed by a newline, which ends its last walk as the host

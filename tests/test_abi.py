@@ -91,6 +91,14 @@ def test_kernel_level_entry_points_check_arguments_first(sgns_lib):
     assert L.sgns_link_scores(0, 8, fake, 10, fake, 0, fake, None) == sgns.OK  # nothing to do
 
 
+def test_command_line_wildcard_without_match_is_an_error(sgns_lib, tmp_path):
+    import os
+
+    cli = os.path.join(os.path.dirname(sgns.LIB_PATH), "sgns_train")
+    r = subprocess.run([cli, "-train", str(tmp_path / "walks-*.txt")], capture_output=True, text=True)
+    assert r.returncode == 1 and "no walk file matches" in r.stderr
+
+
 def test_walk_text_formatter_writes_the_reference_format():
     """bench.format_walk_text (the text the ingest benchmark parses) is the reference's
     walk format, byte for byte as synth.write_walk_file writes it."""

@@ -115,16 +115,21 @@ def test_text_output_is_the_references(name, sgns_lib, tmp_path):
 
 @pytest.mark.parametrize("name", GOLDEN_CASES)
 def test_command_line_trainer_on_walk_files(name, sgns_lib, tmp_path):
-    """The sgns_train command line on the golden corpus written as a walk file (" %u" per
-    vertex, one walk per line) reproduces the reference's embedding file byte for byte."""
+    """The sgns_train command line on the golden corpus written as walk files (" %u" per
+    vertex, one walk per line; named by a wildcard) reproduces the reference's embedding
+    file byte for byte."""
     import subprocess
     import synth
 
     meta, corpus = golden(name)
     if corpus[0] == -1 or np.any((corpus[:-1] == -1) & (corpus[1:] == -1)):
         pytest.skip("holds an empty walk, which a walk file cannot express")
-    walks = str(tmp_path / "walks.txt")
-    synth.write_walk_file(corpus, walks)
+    # two files split at a walk boundary, named by a wildcard (sorted: walks-0, walks-1)
+    ends = np.flatnonzero(corpus == -1)
+    cut = int(ends[len(ends) // 2]) + 1
+    synth.write_walk_file(corpus[:cut], str(tmp_path / "walks-0.txt"))
+    synth.write_walk_file(corpus[cut:], str(tmp_path / "walks-1.txt"))
+    walks = str(tmp_path / "walks-*.txt")
     out = str(tmp_path / "emb.txt")
     cli = os.path.join(os.path.dirname(sgns.LIB_PATH), "sgns_train")
     cmd = [cli, "-train", walks, "-eoutput", out, "-size", str(meta["d"]), "-window", str(meta["window"]),
