@@ -73,8 +73,10 @@ struct sgns_handle {
 
 namespace {
 
-std::mutex g_create_err_mx;
-std::string g_create_err;
+// message of the calling thread's last failed call without a handle (sgns_create, the
+// kernel-level entry points); per thread, so the pointer sgns_last_error(NULL) returns
+// stays valid until that thread's next failure
+thread_local std::string g_create_err;
 
 sgns_status fail(sgns_handle* h, sgns_status st, const char* fmt, ...) {
   char buf[512];
@@ -84,7 +86,6 @@ sgns_status fail(sgns_handle* h, sgns_status st, const char* fmt, ...) {
   va_end(ap);
   if (h) h->err = buf;
   else {
-    std::lock_guard<std::mutex> g(g_create_err_mx);
     g_create_err = buf;
   }
   return st;
@@ -436,7 +437,6 @@ int report_error(int status, const char* fmt, ...) {
   va_start(ap, fmt);
   vsnprintf(buf, sizeof buf, fmt, ap);
   va_end(ap);
-  std::lock_guard<std::mutex> g(g_create_err_mx);
   g_create_err = buf;
   return status;
 }
@@ -591,7 +591,6 @@ void sgns_destroy(sgns_handle* h) {
 
 const char* sgns_last_error(const sgns_handle* h) {
   if (h) return h->err.c_str();
-  std::lock_guard<std::mutex> g(g_create_err_mx);
   return g_create_err.c_str();
 }
 

@@ -109,7 +109,9 @@ typedef struct sgns_handle sgns_handle;
 /* Creates a trainer on opt->device.  Replaces dsgl()'s flag scan and globals. */
 sgns_status sgns_create(const sgns_options* opt, sgns_handle** out);
 void sgns_destroy(sgns_handle* h);
-/* Message of the last failed call on h (or of the last failed sgns_create when h is NULL). */
+/* Message of the last failed call on h; with h NULL, of the calling thread's last failed
+ * call that has no handle (sgns_create, sgns_options_from_args, the kernel-level entry
+ * points).  Valid until the next failure on h, or of that thread. */
 const char* sgns_last_error(const sgns_handle* h);
 
 /* Vocabulary from per-vertex occurrence counts (the reference's vertex_cn), then the

@@ -91,6 +91,33 @@ def test_kernel_level_entry_points_check_arguments_first(sgns_lib):
     assert L.sgns_link_scores(0, 8, fake, 10, fake, 0, fake, None) == sgns.OK  # nothing to do
 
 
+def test_handle_less_errors_are_per_thread(sgns_lib):
+    """sgns_last_error(NULL) reports the calling thread's own last failure."""
+    import ctypes
+    import threading
+
+    L = sgns.lib()
+    n_tok, mx = ctypes.c_int64(), ctypes.c_int64()
+    seen = {}
+    both_failed = threading.Barrier(2)
+
+    def worker(name, fn):
+        assert fn() == sgns.EINVAL
+        both_failed.wait()  # the other thread has failed too before either reads
+        seen[name] = L.sgns_last_error(None)
+
+    fake = ctypes.c_void_p(16)
+    t1 = threading.Thread(target=worker, args=("parse", lambda: L.sgns_parse_walks(
+        None, 5, None, 0, ctypes.byref(n_tok), ctypes.byref(mx), None)))
+    t2 = threading.Thread(target=worker, args=("score", lambda: L.sgns_link_scores(
+        7, 8, fake, 10, fake, 1, fake, None)))
+    for t in (t1, t2):
+        t.start()
+    for t in (t1, t2):
+        t.join()
+    assert b"walk-parse" in seen["parse"] and b"link-score" in seen["score"]
+
+
 def test_command_line_wildcard_without_match_is_an_error(sgns_lib, tmp_path):
     import os
 
