@@ -216,7 +216,7 @@ def run_reference(args, wl):
               "this host: its sources are not shipped to it)" % (min(nw, len(ends)), cut, args.workload))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": {"workload": args.workload + " (CPU sample)", **TRAIN},
             "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -737,7 +737,7 @@ def main():
                 "kernel_ms": float(np.mean(kernel_ms))}
     line = {"metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * elapsed_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Chung-Lu stand-in for LiveJournal; random walks)",
             "config": {"workload": "%s: Chung-Lu V=%d E=%d gamma=%.1f, 10 walks/vertex geometric(mean %d, cap %d) "
                                    "on the 90%% training graph, %d tokens per rank" %
