@@ -329,8 +329,60 @@ sgns_status run_plain(sgns_handle* h, int workers, float* ms_out) {
 
 // Autotuner: times each CTA shape of the persistent engine on a prefix of the corpus,
 // on scratch copies of the tables, and keeps the fastest (pairs per second).
+// Autotuner cache: with SGNS_TUNE_CACHE naming a file, the chosen CTA shape is kept per
+// device model and problem shape ("key<TAB>warps_per_cta" lines) and reused by later runs.
+// The file is only an optimisation: any error reading or writing it is ignored.
+std::string tune_key(const sgns_handle* h) {
+  cudaDeviceProp prop{};
+  if (cudaGetDeviceProperties(&prop, h->opt.device) != cudaSuccess) prop.name[0] = 0;
+  char key[384];
+  snprintf(key, sizeof key, "%s|sms=%d|d=%d|w=%d|K=%d|storage=%d|lmax=%d|workers=%d", prop.name, h->num_sms,
+           h->opt.size, h->opt.window, h->opt.negative, h->opt.storage, h->lmax, h->opt.workers);
+  for (char* c = key; *c; c++)
+    if (*c == '\t' || *c == '\n') *c = ' ';
+  return key;
+}
+int tune_cache_lookup(const std::string& key) {
+  const char* path = getenv("SGNS_TUNE_CACHE");
+  if (!path || !*path) return 0;
+  FILE* f = fopen(path, "r");
+  if (!f) return 0;
+  char line[512];
+  int wpc = 0;
+  while (fgets(line, sizeof line, f)) {
+    char* tab = strchr(line, '\t');
+    if (!tab) continue;
+    *tab = 0;
+    if (key == line) wpc = atoi(tab + 1);  // the last entry for a key wins
+  }
+  fclose(f);
+  return wpc >= 1 && wpc <= 8 ? wpc : 0;
+}
+void tune_cache_store(const std::string& key, int wpc) {
+  const char* path = getenv("SGNS_TUNE_CACHE");
+  if (!path || !*path) return;
+  if (FILE* f = fopen(path, "a")) {
+    fprintf(f, "%s\t%d\n", key.c_str(), wpc);
+    fclose(f);
+  }
+}
+
 sgns_status autotune(sgns_handle* h) {
   const sgns_options& o = h->opt;
+  const std::string key = tune_key(h);
+  if (o.warps_per_cta <= 0) {
+    if (const int cached = tune_cache_lookup(key)) {
+      int workers = o.workers;
+      if (!workers && persistent_shape(h, cached, &workers) != SGNS_OK) workers = 0;
+      if (workers > 0) {
+        h->wpc = cached;
+        h->workers = workers;
+        h->tuned = true;
+        if (o.debug > 0) fprintf(stderr, "sgns: persistent engine shape from the tuning cache: %d warps/CTA\n", cached);
+        return SGNS_OK;
+      }
+    }
+  }
   if (o.warps_per_cta > 0) {
     h->wpc = o.warps_per_cta;
     h->workers = o.workers;
@@ -388,6 +440,7 @@ sgns_status autotune(sgns_handle* h) {
   h->wpc = best_wpc;
   h->workers = best_workers;
   h->tuned = true;
+  tune_cache_store(key, best_wpc);
   if (o.debug > 0)
     fprintf(stderr, "sgns: autotuned persistent engine: %d warps/CTA, %d workers\n", h->wpc, h->workers);
   return SGNS_OK;

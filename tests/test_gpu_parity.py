@@ -242,6 +242,28 @@ def test_pinned_host_corpus_is_read_in_place(sgns_lib):
         assert e.value.status == sgns.EINVAL
 
 
+def test_autotuner_cache_file(sgns_lib, tmp_path, monkeypatch):
+    """With SGNS_TUNE_CACHE set, the autotuner records its choice per device and shape and a
+    later run takes the recorded shape instead of tuning again."""
+    cache = tmp_path / "tune.txt"
+    monkeypatch.setenv("SGNS_TUNE_CACHE", str(cache))
+    cfg, corpus, _ = case("cl_d128")
+    counts = np.bincount(corpus[corpus >= 0], minlength=cfg["V"]).astype(np.int32)
+
+    def run():
+        with sgns.Trainer(size=cfg["d"], window=cfg["window"], negative=cfg["negative"], table_size=1000000,
+                          debug=0, storage="bf16") as t:
+            t.set_vocab(counts)
+            return t.train_corpus(corpus).warps_per_cta
+
+    first = run()
+    lines = cache.read_text().splitlines()
+    assert len(lines) == 1 and lines[0].endswith("\t%d" % first)
+    planted = 3 if first != 3 else 2  # the last entry of a key wins
+    cache.write_text(lines[0].rsplit("\t", 1)[0] + "\t%d\n" % planted, encoding="utf-8")
+    assert run() == planted
+
+
 @pytest.mark.parametrize("engine,policy", [("plain", 0), ("persistent", 1)])
 def test_many_workers_follow_the_reference_control_flow(engine, policy, sgns_lib, oracle_mod):
     """Hogwild workers race on table rows, but every worker's control flow (slice,
