@@ -242,6 +242,35 @@ def test_pinned_host_corpus_is_read_in_place(sgns_lib):
         assert e.value.status == sgns.EINVAL
 
 
+def random_config(seed):
+    """A random configuration and power-law corpus (the generator of the oracle's
+    differential test against the reference)."""
+    rng = np.random.default_rng(seed)
+    V = int(rng.integers(1001, 2500))
+    w = (np.arange(V) + rng.uniform(2, 30)) ** -rng.uniform(0.6, 1.2)
+    w /= w.sum()
+    toks = []
+    for _ in range(int(rng.integers(50, 250))):
+        toks.extend(rng.choice(V, size=int(rng.integers(1, 90)), p=w).tolist())
+        toks.append(-1)
+    cfg = dict(V=V, d=int(rng.choice([4, 8, 12, 16, 20, 32, 36, 64])), window=int(rng.integers(1, 12)),
+               negative=int(rng.integers(0, 11)), iter=int(rng.integers(1, 3)),
+               sample=float(rng.choice([0.0, 1e-4, 1e-3, 1e-2])), alpha=float(rng.choice([0.01, 0.025, 0.05])))
+    return cfg, np.array(toks, dtype=np.int32)
+
+
+@pytest.mark.parametrize("seed", [101, 303, 1002, 1003, 2054, 2192])
+@pytest.mark.parametrize("engine,storage", [("plain", "fp32"), ("persistent", "fp32"), ("persistent", "bf16")])
+def test_engines_match_oracle_on_random_configs(seed, engine, storage, sgns_lib, oracle_mod):
+    cfg, corpus = random_config(seed)
+    wih, woh, st, _ = gpu_train(cfg, corpus, engine, storage, workers=0, wpc=0, mode="exact")
+    policy = oracle_mod.POLICY_REF if engine == "plain" else oracle_mod.POLICY_WINDOW
+    owih, owoh, ost = oracle_train(oracle_mod, cfg, corpus, policy, storage)
+    assert (st.steps, st.pairs, st.word_count_actual) == (ost["steps"], ost["pairs"], ost["word_count_actual"]), cfg
+    assert np.array_equal(wih.view(np.uint32), owih.view(np.uint32)), (cfg, np.abs(wih - owih).max())
+    assert np.array_equal(woh.view(np.uint32), owoh.view(np.uint32)), (cfg, np.abs(woh - owoh).max())
+
+
 def test_autotuner_cache_file(sgns_lib, tmp_path, monkeypatch):
     """With SGNS_TUNE_CACHE set, the autotuner records its choice per device and shape and a
     later run takes the recorded shape instead of tuning again."""
