@@ -86,7 +86,9 @@ typedef struct sgns_stats {
   uint64_t steps;              /* minibatches trained (one per target pair of walks) */
   uint64_t pairs;              /* (context, target) pairs = input rows over all steps */
   uint64_t word_count_actual;  /* tokens consumed, as the reference counts them      */
-  uint64_t row_bytes;          /* algorithmic row traffic of the run  */
+  uint64_t row_bytes;          /* algorithmic row traffic of the run: every step reads
+                                  and writes its input and output rows once,
+                                  2 (pairs + output_rows) d elem_bytes            */
   double loss;                 /* sum of SGNS losses (compute_loss = 1), fp64        */
   float final_alpha;
   float train_ms;              /* device time of the last training call              */
