@@ -88,6 +88,9 @@ sgns_status fail(sgns_handle* h, sgns_status st, const char* fmt, ...) {
   else {
     g_create_err = buf;
   }
+  // a failed allocation or copy also sets the runtime's per-thread last error, which the
+  // launchers read back after their next launch: clear it so it is reported only here
+  if (st == SGNS_ECUDA || st == SGNS_ENOMEM) cudaGetLastError();
   return st;
 }
 
@@ -106,6 +109,29 @@ void dfree(T*& p) {
 }
 
 size_t elem_bytes(const sgns_options& o) { return o.storage == SGNS_STORE_BF16_SR ? 2 : 4; }
+
+// Back to the state before any vocabulary: every buffer sized by V or by the corpus is
+// freed together, so no later call sees some of them and not the others.
+void drop_vocab(sgns_handle* h) {
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  h->graph_key.clear();
+  h->tuned = false;
+  dfree(h->wih);
+  dfree(h->woh);
+  dfree(h->d_row_of);
+  dfree(h->d_ran);
+  dfree(h->d_table);
+  dfree(h->d_corpus);
+  dfree(h->d_ids);
+  h->V = 0;
+  h->train_words = 0;
+  h->n_tokens = h->corpus_cap = 0;
+  h->lmax = 2;  // an empty corpus: the shortest walk the engines stage
+}
 
 // ---- the reference's host set-up, restated (dsgl.hpp:121-147, 246-252, 314-382) ----
 struct VocabVertex {
@@ -393,21 +419,53 @@ sgns_status autotune(sgns_handle* h) {
     h->tuned = true;
     return SGNS_OK;
   }
+  // the trial launches train scratch copies of the tables; the handle's own pointers,
+  // corpus length and pass count are put back on every path out of the search
   const size_t tbytes = (size_t)h->V * o.size * elem_bytes(o);
   void *wih_s = nullptr, *woh_s = nullptr;
-  CU(h, cudaMalloc(&wih_s, tbytes));
-  CU(h, cudaMalloc(&woh_s, tbytes));
-  CU(h, cudaMemcpyAsync(wih_s, h->wih, tbytes, cudaMemcpyDeviceToDevice, h->stream));
-  CU(h, cudaMemcpyAsync(woh_s, h->woh, tbytes, cudaMemcpyDeviceToDevice, h->stream));
   void *wih0 = h->wih, *woh0 = h->woh;
   const int64_t n0 = h->n_tokens;
   const int iter0 = h->opt.iter;
-  h->wih = wih_s;
-  h->woh = woh_s;
-  h->opt.iter = 1;
+  auto restore = [&]() {
+    cudaStreamSynchronize(h->stream);
+    h->wih = wih0;
+    h->woh = woh0;
+    h->n_tokens = n0;
+    h->opt.iter = iter0;
+    dfree(wih_s);
+    dfree(woh_s);
+  };
   double best = -1.0;
   int best_wpc = 1, best_workers = 0;
   sgns_status st = SGNS_OK;
+  cudaError_t e;
+  if ((e = cudaMalloc(&wih_s, tbytes)) != cudaSuccess || (e = cudaMalloc(&woh_s, tbytes)) != cudaSuccess) {
+    // no room for scratch tables: take the most warps per CTA that fit (occupancy is
+    // what bounds this latency-bound kernel), untimed
+    restore();
+    cudaGetLastError();
+    for (int wpc = 8; wpc >= 1 && !best_workers; wpc--) {
+      int workers = 0;
+      if (persistent_shape(h, wpc, &workers) != SGNS_OK) continue;
+      best_wpc = wpc;
+      best_workers = o.workers > 0 ? o.workers : workers;
+    }
+    if (best_workers == 0) return fail(h, SGNS_EINVAL, "no persistent-engine shape fits this configuration");
+    h->wpc = best_wpc;
+    h->workers = best_workers;
+    h->tuned = true;
+    if (o.debug > 0)
+      fprintf(stderr, "sgns: no memory for autotuning; persistent engine at %d warps/CTA\n", best_wpc);
+    return SGNS_OK;
+  }
+  if ((e = cudaMemcpyAsync(wih_s, h->wih, tbytes, cudaMemcpyDeviceToDevice, h->stream)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(woh_s, h->woh, tbytes, cudaMemcpyDeviceToDevice, h->stream)) != cudaSuccess) {
+    restore();
+    return fail(h, SGNS_ECUDA, "autotuner table copies: %s", cudaGetErrorString(e));
+  }
+  h->wih = wih_s;
+  h->woh = woh_s;
+  h->opt.iter = 1;
   for (int wpc = 1; wpc <= 8; wpc++) {
     int workers = 0;
     st = persistent_shape(h, wpc, &workers);
@@ -421,7 +479,10 @@ sgns_status autotune(sgns_handle* h) {
     float ms = 0.f;
     st = run_persistent(h, workers, wpc, false, &ms);
     if (st) break;
-    CU(h, cudaMemcpy(h->h_ctr, h->d_ctr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost));
+    if ((e = cudaMemcpy(h->h_ctr, h->d_ctr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost)) != cudaSuccess) {
+      st = fail(h, SGNS_ECUDA, "autotuner counters: %s", cudaGetErrorString(e));
+      break;
+    }
     const double rate = ms > 0 ? (double)h->h_ctr->pairs / ms : 0.0;
     if (rate > best) {
       best = rate;
@@ -429,12 +490,7 @@ sgns_status autotune(sgns_handle* h) {
       best_workers = workers;
     }
   }
-  h->wih = wih0;
-  h->woh = woh0;
-  h->n_tokens = n0;
-  h->opt.iter = iter0;
-  cudaFree(wih_s);
-  cudaFree(woh_s);
+  restore();
   if (st) return st;
   if (best_workers == 0) return fail(h, SGNS_EINVAL, "no persistent-engine shape fits this configuration");
   h->wpc = best_wpc;
@@ -663,8 +719,7 @@ sgns_status sgns_set_vocab(sgns_handle* h, const int32_t* counts, int64_t V) {
     tw += (uint64_t)counts[i];
   }
   std::sort(v.begin(), v.end(), [](VocabVertex a, VocabVertex b) { return a.cn > b.cn; });
-  h->V = V;
-  h->train_words = tw;
+  drop_vocab(h);
   h->order.resize(V);
   h->row_of.resize(V);
   h->cn_sorted.resize(V);
@@ -683,30 +738,33 @@ sgns_status sgns_set_vocab(sgns_handle* h, const int32_t* counts, int64_t V) {
     const float ratio = st / (float)counts[w];
     ran[w] = sqrtf(ratio) + ratio;
   }
-  if (h->graph) {
-    cudaGraphExecDestroy(h->graph);
-    h->graph = nullptr;
-  }
-  h->tuned = false;
-  dfree(h->wih);
-  dfree(h->woh);
-  dfree(h->d_row_of);
-  dfree(h->d_ran);
-  dfree(h->d_table);
-  dfree(h->d_corpus);
-  dfree(h->d_ids);
-  h->n_tokens = h->corpus_cap = 0;
+  // a failure below leaves the handle without a vocabulary (as before the first call)
   const size_t tbytes = (size_t)V * h->opt.size * elem_bytes(h->opt);
   cudaError_t e;
-  if ((e = cudaMalloc(&h->wih, tbytes)) != cudaSuccess || (e = cudaMalloc(&h->woh, tbytes)) != cudaSuccess)
+  if ((e = cudaMalloc(&h->wih, tbytes)) != cudaSuccess || (e = cudaMalloc(&h->woh, tbytes)) != cudaSuccess) {
+    drop_vocab(h);
+    cudaGetLastError();
     return fail(h, SGNS_ENOMEM, "embedding tables (2 x %zu bytes): %s", tbytes, cudaGetErrorString(e));
-  CU(h, cudaMalloc(&h->d_row_of, sizeof(int32_t) * V));
-  CU(h, cudaMalloc(&h->d_ran, sizeof(float) * V));
-  CU(h, cudaMalloc(&h->d_table, sizeof(int32_t) * table.size()));
-  CU(h, cudaMemcpy(h->d_row_of, h->row_of.data(), sizeof(int32_t) * V, cudaMemcpyHostToDevice));
-  CU(h, cudaMemcpy(h->d_ran, ran.data(), sizeof(float) * V, cudaMemcpyHostToDevice));
-  CU(h, cudaMemcpy(h->d_table, table.data(), sizeof(int32_t) * table.size(), cudaMemcpyHostToDevice));
-  return sgns_reset_model(h);
+  }
+  if ((e = cudaMalloc(&h->d_row_of, sizeof(int32_t) * V)) != cudaSuccess ||
+      (e = cudaMalloc(&h->d_ran, sizeof(float) * V)) != cudaSuccess ||
+      (e = cudaMalloc(&h->d_table, sizeof(int32_t) * table.size())) != cudaSuccess) {
+    drop_vocab(h);
+    cudaGetLastError();
+    return fail(h, SGNS_ENOMEM, "vocabulary tables: %s", cudaGetErrorString(e));
+  }
+  if ((e = cudaMemcpy(h->d_row_of, h->row_of.data(), sizeof(int32_t) * V, cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemcpy(h->d_ran, ran.data(), sizeof(float) * V, cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemcpy(h->d_table, table.data(), sizeof(int32_t) * table.size(), cudaMemcpyHostToDevice)) !=
+          cudaSuccess) {
+    drop_vocab(h);
+    return fail(h, SGNS_ECUDA, "vocabulary upload: %s", cudaGetErrorString(e));
+  }
+  h->V = V;
+  h->train_words = tw;
+  const sgns_status rs = sgns_reset_model(h);
+  if (rs) drop_vocab(h);
+  return rs;
 }
 
 sgns_status sgns_reset_model(sgns_handle* h) {

@@ -329,3 +329,62 @@ def test_empty_and_degenerate_corpora(sgns_lib):
             st = t.train_corpus(np.array([-1, -1, 3, -1, 4, -1], np.int32))  # only length-1 walks
             assert st.steps == 0
             assert np.array_equal(t.embeddings(0), w0)
+
+
+def _hold_all_but(nbytes):
+    """Device memory held by torch so that about nbytes stay free."""
+    import torch
+
+    free, _ = torch.cuda.mem_get_info()
+    return torch.empty(max(0, free - nbytes), dtype=torch.uint8, device="cuda")
+
+
+def test_failed_vocabulary_leaves_the_handle_without_one(sgns_lib):
+    """Tables that do not fit: sgns_set_vocab fails with ENOMEM and leaves the handle as
+    before any vocabulary (training refused with ESTATE, nothing half-allocated); a
+    vocabulary that fits then trains."""
+    import torch
+
+    opt = sgns.default_options(size=256, window=2, negative=2, iter=1, debug=0, table_size=1000, sample=0.0,
+                               workers=1, warps_per_cta=1)
+    with sgns.Trainer(opt) as t:
+        hold = _hold_all_but(3 << 29)  # 1.5 GiB free; the two tables need 2 GiB
+        try:
+            with pytest.raises(sgns.SgnsError) as e:
+                t.set_vocab(np.ones(1 << 20, np.int32))
+            assert e.value.status == sgns.ENOMEM
+        finally:
+            del hold
+            torch.cuda.empty_cache()
+        assert t.vocab_size == 0
+        with pytest.raises(sgns.SgnsError) as e:
+            t.train()
+        assert e.value.status == sgns.ESTATE
+        t.set_vocab(np.ones(10, np.int32))
+        walks = np.random.default_rng(3).integers(0, 10, (30, 6))
+        st = t.train_corpus(np.hstack([walks, -np.ones((30, 1), np.int64)]).ravel().astype(np.int32))
+        assert st.steps > 0 and np.isfinite(t.embeddings(0)).all()
+
+
+def test_autotuner_without_room_for_scratch_tables(sgns_lib):
+    """When the autotuner's scratch copies of the tables do not fit, the engine runs at the
+    most warps per CTA that fit instead of failing, and trains the same control flow."""
+    import torch
+
+    rng = np.random.default_rng(7)
+    V = 1 << 20
+    corpus = np.concatenate([np.append(rng.integers(0, V, 60), -1) for _ in range(4000)]).astype(np.int32)
+    counts = np.bincount(corpus[corpus >= 0], minlength=V).astype(np.int32)
+    counts[counts == 0] = 1
+    opt = sgns.default_options(size=256, window=5, negative=5, iter=1, debug=0, table_size=1000000)
+    with sgns.Trainer(opt) as t:
+        t.set_vocab(counts)  # two 1 GiB tables
+        t.upload(corpus)
+        hold = _hold_all_but(3 << 29)  # room for one scratch table, not two
+        try:
+            st = t.train()
+        finally:
+            del hold
+            torch.cuda.empty_cache()
+        assert 1 <= st.warps_per_cta <= 8 and st.steps > 0 and st.pairs > 0
+        assert np.isfinite(t.embeddings(0)).all() and np.isfinite(t.embeddings(1)).all()
