@@ -440,17 +440,20 @@ sgns_status autotune(sgns_handle* h) {
   sgns_status st = SGNS_OK;
   cudaError_t e;
   if ((e = cudaMalloc(&wih_s, tbytes)) != cudaSuccess || (e = cudaMalloc(&woh_s, tbytes)) != cudaSuccess) {
-    // no room for scratch tables: take the most warps per CTA that fit (occupancy is
-    // what bounds this latency-bound kernel), untimed
+    // no room for scratch tables: take, untimed, the shape with the most resident
+    // workers (warps per SM bound this latency-bound kernel); ties go to the wider CTA
     restore();
     cudaGetLastError();
-    for (int wpc = 8; wpc >= 1 && !best_workers; wpc--) {
+    for (int wpc = 1; wpc <= 8; wpc++) {
       int workers = 0;
       if (persistent_shape(h, wpc, &workers) != SGNS_OK) continue;
-      best_wpc = wpc;
-      best_workers = o.workers > 0 ? o.workers : workers;
+      if (workers >= best_workers) {
+        best_wpc = wpc;
+        best_workers = workers;
+      }
     }
     if (best_workers == 0) return fail(h, SGNS_EINVAL, "no persistent-engine shape fits this configuration");
+    if (o.workers > 0) best_workers = o.workers;
     h->wpc = best_wpc;
     h->workers = best_workers;
     h->tuned = true;
