@@ -7,7 +7,8 @@
 // and writes the text embedding of my_saveModel (dsgl.hpp:1443-1461).
 //
 // Additional flags: -vertices V (vocabulary size; default max id + 1), -storage fp32|bf16,
-// -engine plain|persistent, -workers N, -warps-per-cta N, -table-size N, -seed N, -device N.
+// -engine plain|persistent, -mode hogwild|exact, -workers N, -warps-per-cta N, -table-size N,
+// -seed N, -device N, -loss 0|1.
 #include <glob.h>
 
 #include <cstdio>
@@ -55,7 +56,8 @@ int main(int argc, char** argv) {
             "usage: %s -train <walk file> [-train ...] [-eoutput <embedding file>] [-size d] [-window w]\n"
             "          [-negative K] [-batch-size B] [-sample s] [-alpha a] [-min-count m] [-iter n]\n"
             "          [-threads t] [-debug n] [-binary 0|1] [-vertices V] [-storage fp32|bf16]\n"
-            "          [-engine plain|persistent] [-workers N] [-table-size N] [-seed N] [-device N]\n",
+            "          [-engine plain|persistent] [-mode hogwild|exact] [-workers N] [-warps-per-cta N]\n"
+            "          [-table-size N] [-seed N] [-device N] [-loss 0|1]\n",
             argv[0]);
     return 2;
   }
