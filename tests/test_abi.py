@@ -1,4 +1,6 @@
 """The C ABI library without a GPU: symbols, option parsing, arithmetic helpers."""
+import ctypes
+import os
 import random
 import subprocess
 
@@ -16,6 +18,23 @@ def test_every_declared_symbol_is_exported(sgns_lib):
     missing = [n for n in names if n not in exported]
     assert not missing, missing
 
+
+
+@pytest.mark.parametrize("ctype,cname", [(sgns.Options, "sgns_options"), (sgns.Stats, "sgns_stats")])
+def test_ctypes_structs_match_the_header(ctype, cname, tmp_path):
+    """The binding's struct mirrors have the C layout of include/sgns.h: size and the
+    offset of every field, as a C compiler lays them out."""
+    fields = [f for f, _ in ctype._fields_]
+    src = tmp_path / "layout.c"
+    src.write_text("#include <stddef.h>\n#include <stdio.h>\n#include \"sgns.h\"\nint main(void) {\n"
+                   + '  printf("%%zu\\n", sizeof(%s));\n' % cname
+                   + "".join('  printf("%%zu\\n", offsetof(%s, %s));\n' % (cname, f) for f in fields)
+                   + "  return 0;\n}\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.dirname(sgns.HEADER), str(src), "-o", str(exe)], check=True)
+    out = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert out[0] == ctypes.sizeof(ctype)
+    assert out[1:] == [getattr(ctype, f).offset for f in fields]
 
 def test_defaults_are_the_references(sgns_lib):
     o = sgns.default_options()
