@@ -65,3 +65,21 @@ def test_init_matches_reference_lcg(oracle_mod):
         r = (r * 25214903917 + 11) % (1 << 64)
         v = np.float32((np.float32(r & 0xFFFF) / np.float32(65536.0)) - np.float32(0.5)) / np.float32(d)
         assert w[i] == np.float32(v)
+
+
+@pytest.mark.parametrize("policy", [0, 1])
+@pytest.mark.parametrize("name", ["basic", "d128_w10"])
+def test_control_flow_does_not_depend_on_d(name, policy, oracle_mod):
+    """Steps, pairs and word counts depend on the corpus, the configuration and the worker
+    count, not on the table values or d: the premise of the full-size GPU check, which
+    counts with the oracle at d = 4.  Many Hogwild workers on several threads."""
+    meta, corpus, _ = load(name)
+    counts = np.bincount(corpus[corpus >= 0], minlength=meta["V"]).astype(np.int32)
+    runs = []
+    for d, storage in ((4, oracle_mod.STORE_F32), (meta["d"], oracle_mod.STORE_F32), (64, oracle_mod.STORE_BF16)):
+        _, _, st = oracle_mod.train(corpus, counts, d=d, window=meta["window"], negative=meta["negative"],
+                                    iter=meta["iter"], workers=23, threads=4, table_threads=meta["table_threads"],
+                                    policy=policy, storage=storage, table_size=meta["table_size"],
+                                    sample=meta["sample"], alpha=meta["alpha"])
+        runs.append((st["steps"], st["pairs"], st["word_count_actual"]))
+    assert runs[0][0] > 0 and runs[0] == runs[1] == runs[2], runs
