@@ -168,6 +168,45 @@ void build_unigram_table(const std::vector<int32_t>& cn, int64_t table_size, int
   }
 }
 
+// The reference's host set-up of a vocabulary: rows sorted by count, descending, with
+// std::sort (dsgl.hpp:246-252, 314-382), the unigram table (dsgl.hpp:121-147) and the
+// subsampling keep thresholds sqrt(r) + r, r = sample * train_words / count (dsgl.hpp:
+// 923-924), indexed by sorted row as the reference indexes its vertex-indexed count array.
+struct HostVocab {
+  std::vector<uint32_t> order;
+  std::vector<int32_t> row_of, cn_sorted, table;
+  std::vector<float> ran;
+  uint64_t train_words = 0;
+};
+
+void build_host_vocab(const int32_t* counts, int64_t V, float sample, int64_t table_size, int threads,
+                      HostVocab& hv) {
+  std::vector<VocabVertex> v(V);
+  uint64_t tw = 0;
+  for (int64_t i = 0; i < V; i++) {
+    v[i].cn = counts[i];
+    v[i].id = (uint32_t)i;
+    tw += (uint64_t)counts[i];
+  }
+  std::sort(v.begin(), v.end(), [](VocabVertex a, VocabVertex b) { return a.cn > b.cn; });
+  hv.order.resize(V);
+  hv.row_of.resize(V);
+  hv.cn_sorted.resize(V);
+  for (int64_t r = 0; r < V; r++) {
+    hv.order[r] = v[r].id;
+    hv.row_of[v[r].id] = (int32_t)r;
+    hv.cn_sorted[r] = v[r].cn;
+  }
+  build_unigram_table(hv.cn_sorted, table_size, threads, hv.table);
+  hv.ran.resize(V);
+  const float st = sample * (float)tw;
+  for (int64_t w = 0; w < V; w++) {
+    const float ratio = st / (float)counts[w];
+    hv.ran[w] = sqrtf(ratio) + ratio;
+  }
+  hv.train_words = tw;
+}
+
 void build_exp_table(float* t) {  // dsgl.hpp:1557-1562
   for (int i = 0; i < kExpTableSize + 1; i++) {
     const float e = expf(((float)i / (float)kExpTableSize * 2 - 1) * kMaxExp);
@@ -557,6 +596,25 @@ int report_error(int status, const char* fmt, ...) {
 // ===================================================================================
 extern "C" {
 
+// Host set-up of sgns_set_vocab without a device (declared in sgns_internal.h, not in the
+// public header): the CPU tests compare it with the oracle.
+int32_t sgns_internal_host_vocab(const int32_t* counts, int64_t V, float sample, int64_t table_size, int32_t threads,
+                                 uint32_t* order, int32_t* table, float* ran, float* exp_table,
+                                 uint64_t* train_words) {
+  if (!counts || V < 1 || V > (int64_t)INT32_MAX || table_size < 1 || table_size > (int64_t)INT32_MAX)
+    return SGNS_EINVAL;
+  for (int64_t i = 0; i < V; i++)
+    if (counts[i] < 0) return SGNS_EINVAL;
+  HostVocab hv;
+  build_host_vocab(counts, V, sample, table_size, threads, hv);
+  if (order) std::memcpy(order, hv.order.data(), sizeof(uint32_t) * V);
+  if (table) std::memcpy(table, hv.table.data(), sizeof(int32_t) * table_size);
+  if (ran) std::memcpy(ran, hv.ran.data(), sizeof(float) * V);
+  if (exp_table) build_exp_table(exp_table);
+  if (train_words) *train_words = hv.train_words;
+  return SGNS_OK;
+}
+
 void sgns_default_options(sgns_options* o) {
   std::memset(o, 0, sizeof *o);
   o->size = 100;  // dsgl.hpp:70
@@ -713,34 +771,15 @@ sgns_status sgns_set_vocab(sgns_handle* h, const int32_t* counts, int64_t V) {
   CU(h, cudaSetDevice(h->opt.device));
   for (int64_t i = 0; i < V; i++)
     if (counts[i] < 0) return fail(h, SGNS_EINVAL, "negative count at vertex %lld", (long long)i);
-  // dsgl.hpp:314-382 and :246-252 -- rows sorted by count, descending (std::sort)
-  std::vector<VocabVertex> v(V);
-  uint64_t tw = 0;
-  for (int64_t i = 0; i < V; i++) {
-    v[i].cn = counts[i];
-    v[i].id = (uint32_t)i;
-    tw += (uint64_t)counts[i];
-  }
-  std::sort(v.begin(), v.end(), [](VocabVertex a, VocabVertex b) { return a.cn > b.cn; });
+  HostVocab hv;
+  build_host_vocab(counts, V, h->opt.sample, h->opt.table_size, h->opt.threads, hv);
   drop_vocab(h);
-  h->order.resize(V);
-  h->row_of.resize(V);
-  h->cn_sorted.resize(V);
-  for (int64_t r = 0; r < V; r++) {
-    h->order[r] = v[r].id;
-    h->row_of[v[r].id] = (int32_t)r;
-    h->cn_sorted[r] = v[r].cn;
-  }
-  std::vector<int32_t> table;
-  build_unigram_table(h->cn_sorted, h->opt.table_size, h->opt.threads, table);
-  // subsampling keep threshold (dsgl.hpp:923-924), indexed by sorted row as the reference
-  // indexes its vertex-indexed count array
-  std::vector<float> ran(V);
-  const float st = h->opt.sample * (float)tw;
-  for (int64_t w = 0; w < V; w++) {
-    const float ratio = st / (float)counts[w];
-    ran[w] = sqrtf(ratio) + ratio;
-  }
+  h->order = std::move(hv.order);
+  h->row_of = std::move(hv.row_of);
+  h->cn_sorted = std::move(hv.cn_sorted);
+  const std::vector<int32_t>& table = hv.table;
+  const std::vector<float>& ran = hv.ran;
+  const uint64_t tw = hv.train_words;
   // a failure below leaves the handle without a vocabulary (as before the first call)
   const size_t tbytes = (size_t)V * h->opt.size * elem_bytes(h->opt);
   cudaError_t e;

@@ -200,3 +200,11 @@ cudaError_t launch_adjoint(int dtype, int d, int n, int64_t V, int64_t total_in,
                            int imax, int omax, cudaStream_t s);
 
 }  // namespace sgns
+
+// Host set-up of sgns_set_vocab (sorted rows, unigram table, subsampling thresholds, sigmoid
+// table) without a device, exported for the CPU tests; not part of include/sgns.h.  Any
+// output pointer may be null.  Returns SGNS_EINVAL for V or table_size outside
+// [1, 2^31 - 1] or a negative count.
+extern "C" int32_t sgns_internal_host_vocab(const int32_t* counts, int64_t V, float sample, int64_t table_size,
+                                            int32_t threads, uint32_t* order, int32_t* table, float* ran,
+                                            float* exp_table, uint64_t* train_words);

@@ -94,6 +94,9 @@ def lib():
         L.sgns_link_scores.argtypes = [i32, i32, vp, i64, vp, i64, vp, vp]
         L.sgns_loss_adjoint.argtypes = [i32, i32, i64, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp,
                                         ctypes.POINTER(i64), vp, vp, ctypes.POINTER(i64), vp]
+        L.sgns_internal_host_vocab.argtypes = [vp, i64, ctypes.c_float, i64, i32, vp, vp, vp, vp,
+                                               ctypes.POINTER(ctypes.c_uint64)]
+        L.sgns_internal_host_vocab.restype = i32
         for name in header_functions():  # every declared entry point must be exported
             getattr(L, name)
         _lib = L
@@ -280,3 +283,19 @@ def loss_adjoint(dtype, d, V, in_ptr, in_ids, in_first, out_ptr, out_ids, out_me
                                    ctypes.byref(n_in), grad_out_ids.data_ptr(), grad_out.data_ptr(),
                                    ctypes.byref(n_out), ctypes.c_void_p(stream)))
     return n_in.value, n_out.value
+
+
+def host_vocab(counts, sample, table_size, threads):
+    """The host set-up sgns_set_vocab performs, run on the CPU without a device: (order of the
+    count-sorted rows, unigram table, subsampling keep thresholds, sigmoid table,
+    train_words)."""
+    counts = np.ascontiguousarray(counts, dtype=np.int32)
+    V = len(counts)
+    order = np.zeros(V, np.uint32)
+    table = np.zeros(table_size, np.int32)
+    ran = np.zeros(V, np.float32)
+    exp = np.zeros(1001, np.float32)
+    tw = ctypes.c_uint64()
+    _check(lib().sgns_internal_host_vocab(_ptr(counts), V, sample, table_size, threads, _ptr(order), _ptr(table),
+                                          _ptr(ran), _ptr(exp), ctypes.byref(tw)))
+    return order, table, ran, exp, tw.value

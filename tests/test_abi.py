@@ -224,3 +224,35 @@ def test_bf16_stochastic_rounding_is_unbiased():
     v = ((np.uint64(u) + r) >> np.uint64(16)).astype(np.uint32) << 16
     mean = v.view(np.float32).astype(np.float64).mean()
     assert abs(mean - float(x)) < 2 ** -9 * 0.01
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_host_vocabulary_setup_equals_the_oracle(seed, sgns_lib, oracle_mod):
+    """The library's host set-up of a vocabulary (what sgns_set_vocab uploads) against the
+    oracle: row order under std::sort with many tied counts and zero counts, the unigram
+    table, the sigmoid table bit for bit; the keep thresholds against a float32
+    restatement of dsgl.hpp:923-924 (sqrt(r) + r, r = sample * train_words / count)."""
+    rng = np.random.default_rng(seed)
+    V = int(rng.integers(1001, 5000))
+    counts = np.minimum(rng.zipf(1.6, V), 5000).astype(np.int32) - (rng.random(V) < 0.05).astype(np.int32)
+    sample, table_size, threads = [1e-3, 1e-4, 0.0][seed], int(rng.integers(10_000, 300_000)), [1, 4, 12][seed]
+    order, table, ran, exp, tw = sgns.host_vocab(counts, sample, table_size, threads)
+    o_order, _, o_cns, o_tw = oracle_mod.vocab(counts)
+    assert tw == o_tw == int(counts.sum())
+    assert np.array_equal(order, o_order)
+    assert np.array_equal(table, oracle_mod.unigram_table(o_cns, table_size, threads))
+    assert np.array_equal(exp.view(np.uint32), oracle_mod.exp_table().view(np.uint32))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        r = np.float32(sample) * np.float32(tw) / counts.astype(np.float32)
+        want = np.sqrt(r) + r
+    want = want.astype(np.float32)
+    nan = np.isnan(want)  # 0/0 for a zero count with sample 0: compared as NaN, not by bits
+    assert np.array_equal(np.isnan(ran), nan)
+    assert np.array_equal(ran[~nan].view(np.uint32), want[~nan].view(np.uint32))
+
+
+def test_host_vocabulary_setup_rejects_bad_input(sgns_lib):
+    with pytest.raises(sgns.SgnsError):
+        sgns.host_vocab(np.array([3, -1, 2], np.int32), 1e-3, 100, 1)
+    with pytest.raises(sgns.SgnsError):
+        sgns.host_vocab(np.array([3, 1, 2], np.int32), 1e-3, 0, 1)
