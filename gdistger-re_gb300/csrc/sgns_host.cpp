@@ -207,6 +207,46 @@ void build_host_vocab(const int32_t* counts, int64_t V, float sample, int64_t ta
   hv.train_words = tw;
 }
 
+// my_saveModel (dsgl.hpp:1443-1461): "V d\n", then per row "<id> " and d x "%f " (or d raw
+// floats with binary) and "\n", rows in sorted order.  Rows are formatted in parallel
+// chunks and written in order.  Returns SGNS_EIO when the file cannot be written.
+sgns_status write_embedding(const uint32_t* order, const float* w, int64_t V, int d, bool binary, const char* path) {
+  FILE* f = fopen(path, "wb");
+  if (!f) return SGNS_EIO;
+  fprintf(f, "%lld %lld\n", (long long)V, (long long)d);  // dsgl.hpp:1448
+  const int nth = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+  const int64_t chunk = 4096;
+  bool ok = true;
+  for (int64_t r0 = 0; r0 < V && ok; r0 += chunk * nth) {
+    std::vector<std::string> parts(nth);
+    std::vector<std::thread> th;
+    for (int t = 0; t < nth; t++)
+      th.emplace_back([&, t] {
+        const int64_t lo = r0 + t * chunk, hi = std::min<int64_t>(V, lo + chunk);
+        std::string& s = parts[t];
+        char buf[64];
+        for (int64_t r = lo; r < hi; r++) {
+          int n = snprintf(buf, sizeof buf, "%u ", order[r]);
+          s.append(buf, n);
+          if (binary) {
+            s.append(reinterpret_cast<const char*>(&w[(size_t)r * d]), sizeof(float) * d);
+          } else {
+            for (int c = 0; c < d; c++) {
+              n = snprintf(buf, sizeof buf, "%f ", w[(size_t)r * d + c]);
+              s.append(buf, n);
+            }
+          }
+          s.push_back('\n');
+        }
+      });
+    for (auto& t : th) t.join();
+    for (auto& s : parts)
+      if (!s.empty() && fwrite(s.data(), 1, s.size(), f) != s.size()) ok = false;
+  }
+  if (fclose(f) != 0) ok = false;
+  return ok ? SGNS_OK : SGNS_EIO;
+}
+
 void build_exp_table(float* t) {  // dsgl.hpp:1557-1562
   for (int i = 0; i < kExpTableSize + 1; i++) {
     const float e = expf(((float)i / (float)kExpTableSize * 2 - 1) * kMaxExp);
@@ -615,6 +655,14 @@ int32_t sgns_internal_host_vocab(const int32_t* counts, int64_t V, float sample,
   return SGNS_OK;
 }
 
+// The embedding writer of sgns_save_text on host arrays (declared in sgns_internal.h, not
+// in the public header): the CPU tests compare its bytes with the reference's files.
+int32_t sgns_internal_write_embedding(const uint32_t* order, const float* w, int64_t V, int32_t d, int32_t binary,
+                                      const char* path) {
+  if (!order || !w || !path || V < 0 || d < 1) return SGNS_EINVAL;
+  return write_embedding(order, w, V, d, binary != 0, path);
+}
+
 void sgns_default_options(sgns_options* o) {
   std::memset(o, 0, sizeof *o);
   o->size = 100;  // dsgl.hpp:70
@@ -994,42 +1042,9 @@ sgns_status sgns_save_text(sgns_handle* h, const char* path) {
   std::vector<float> w((size_t)V * d);
   sgns_status st = sgns_get_embeddings(h, 0, w.data());
   if (st) return st;
-  FILE* f = fopen(path, "wb");
-  if (!f) return fail(h, SGNS_EIO, "cannot open %s for writing", path);
-  fprintf(f, "%lld %lld\n", (long long)V, (long long)d);  // dsgl.hpp:1448
-  // rows formatted in parallel chunks, written in order (dsgl.hpp:1449-1459)
-  const int nth = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
-  const int64_t chunk = 4096;
-  bool ok = true;
-  for (int64_t r0 = 0; r0 < V && ok; r0 += chunk * nth) {
-    std::vector<std::string> parts(nth);
-    std::vector<std::thread> th;
-    for (int t = 0; t < nth; t++)
-      th.emplace_back([&, t] {
-        const int64_t lo = r0 + t * chunk, hi = std::min<int64_t>(V, lo + chunk);
-        std::string& s = parts[t];
-        char buf[64];
-        for (int64_t r = lo; r < hi; r++) {
-          int n = snprintf(buf, sizeof buf, "%u ", h->order[r]);
-          s.append(buf, n);
-          if (h->opt.binary) {
-            s.append(reinterpret_cast<const char*>(&w[(size_t)r * d]), sizeof(float) * d);
-          } else {
-            for (int c = 0; c < d; c++) {
-              n = snprintf(buf, sizeof buf, "%f ", w[(size_t)r * d + c]);
-              s.append(buf, n);
-            }
-          }
-          s.push_back('\n');
-        }
-      });
-    for (auto& t : th) t.join();
-    for (auto& s : parts)
-      if (!s.empty() && fwrite(s.data(), 1, s.size(), f) != s.size()) ok = false;
-  }
-  if (fclose(f) != 0) ok = false;
-  if (!ok) return fail(h, SGNS_EIO, "write to %s failed", path);
-  return SGNS_OK;
+  st = write_embedding(h->order.data(), w.data(), V, d, h->opt.binary != 0, path);
+  if (st == SGNS_EIO) return fail(h, SGNS_EIO, "cannot write %s", path);
+  return st;
 }
 
 namespace {

@@ -208,3 +208,7 @@ cudaError_t launch_adjoint(int dtype, int d, int n, int64_t V, int64_t total_in,
 extern "C" int32_t sgns_internal_host_vocab(const int32_t* counts, int64_t V, float sample, int64_t table_size,
                                             int32_t threads, uint32_t* order, int32_t* table, float* ran,
                                             float* exp_table, uint64_t* train_words);
+// The writer of sgns_save_text (my_saveModel's format) on host arrays: order (V row ids),
+// w (V x d floats, sorted-row order); exported for the CPU tests.
+extern "C" int32_t sgns_internal_write_embedding(const uint32_t* order, const float* w, int64_t V, int32_t d,
+                                                 int32_t binary, const char* path);

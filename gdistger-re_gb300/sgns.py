@@ -97,6 +97,8 @@ def lib():
         L.sgns_internal_host_vocab.argtypes = [vp, i64, ctypes.c_float, i64, i32, vp, vp, vp, vp,
                                                ctypes.POINTER(ctypes.c_uint64)]
         L.sgns_internal_host_vocab.restype = i32
+        L.sgns_internal_write_embedding.argtypes = [vp, vp, i64, i32, i32, ctypes.c_char_p]
+        L.sgns_internal_write_embedding.restype = i32
         for name in header_functions():  # every declared entry point must be exported
             getattr(L, name)
         _lib = L
@@ -299,3 +301,12 @@ def host_vocab(counts, sample, table_size, threads):
     _check(lib().sgns_internal_host_vocab(_ptr(counts), V, sample, table_size, threads, _ptr(order), _ptr(table),
                                           _ptr(ran), _ptr(exp), ctypes.byref(tw)))
     return order, table, ran, exp, tw.value
+
+
+def write_embedding(order, w, path, binary=False):
+    """The writer of sgns_save_text on host arrays (order: V row ids, w: V x d floats in
+    sorted-row order), run on the CPU without a device."""
+    order = np.ascontiguousarray(order, dtype=np.uint32)
+    w = np.ascontiguousarray(w, dtype=np.float32)
+    _check(lib().sgns_internal_write_embedding(_ptr(order), _ptr(w), w.shape[0], w.shape[1], int(binary),
+                                               str(path).encode()))

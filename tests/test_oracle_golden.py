@@ -83,3 +83,34 @@ def test_control_flow_does_not_depend_on_d(name, policy, oracle_mod):
                                     sample=meta["sample"], alpha=meta["alpha"])
         runs.append((st["steps"], st["pairs"], st["word_count_actual"]))
     assert runs[0][0] > 0 and runs[0] == runs[1] == runs[2], runs
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_embedding_writer_reproduces_reference_file(name, sgns_lib, oracle_mod, tmp_path):
+    """The library's writer of sgns_save_text (my_saveModel, dsgl.hpp:1443-1461), fed the
+    oracle's Wih (equal to the reference's bit for bit), writes the reference's own -eoutput
+    file byte for byte; binary mode writes the raw floats after each id."""
+    import sgns
+
+    meta, corpus, _ = load(name)
+    counts = np.bincount(corpus[corpus >= 0], minlength=meta["V"]).astype(np.int32)
+    wih, _, _ = oracle_mod.train(corpus, counts, d=meta["d"], window=meta["window"], negative=meta["negative"],
+                                 iter=meta["iter"], workers=1, threads=1, table_threads=meta["table_threads"],
+                                 policy=oracle_mod.POLICY_REF, storage=oracle_mod.STORE_F32,
+                                 table_size=meta["table_size"], sample=meta["sample"], alpha=meta["alpha"])
+    order, _, _, _ = oracle_mod.vocab(counts)
+    out = tmp_path / "emb.txt"
+    sgns.write_embedding(order, wih, out)
+    assert hashlib.sha256(out.read_bytes()).hexdigest() == meta["text_sha256"]
+    sgns.write_embedding(order, wih, out, binary=True)
+    raw = out.read_bytes()
+    head = b"%d %d\n" % wih.shape
+    assert raw.startswith(head)
+    pos, d = len(head), wih.shape[1]
+    for r in (0, len(order) - 1):  # first and last rows
+        if r:
+            pos = len(raw) - (len(b"%u " % order[r]) + 4 * d + 1)
+        ident = b"%u " % order[r]
+        assert raw[pos:pos + len(ident)] == ident
+        row = np.frombuffer(raw[pos + len(ident):pos + len(ident) + 4 * d], np.float32)
+        assert np.array_equal(row.view(np.uint32), wih[r].view(np.uint32))
