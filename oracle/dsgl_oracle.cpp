@@ -655,6 +655,8 @@ struct oracle_stats {
   uint64_t steps, pairs, word_count_actual;
   float final_alpha;
   float pad_;
+  double train_seconds;  // the worker loop alone, as the reference's "Train SGNS MPI TIME"
+                         // (dsgl.hpp:1571-1573) excludes preparatory_work
 };
 
 void oracle_build_vocab(const int32_t* counts, int64_t V, uint32_t* order, int32_t* row_of,
@@ -719,6 +721,7 @@ int oracle_train(const oracle_config* cfg, const int32_t* counts, int64_t V, con
   sh.alpha = cfg->alpha;
   sh.steps = 0;
   sh.pairs = 0;
+  const double t0 = omp_get_wtime();
   if (cfg->storage == STORE_F32)
     run_workers<STORE_F32>(sh, (float*)Wih, (float*)Woh, cfg->threads);
   else if (cfg->storage == STORE_BF16)
@@ -732,6 +735,7 @@ int oracle_train(const oracle_config* cfg, const int32_t* counts, int64_t V, con
     stats->pairs = sh.pairs.load();
     stats->word_count_actual = sh.wca.load();
     stats->final_alpha = sh.alpha.load();
+    stats->train_seconds = omp_get_wtime() - t0;
   }
   return 0;
 }

@@ -26,7 +26,7 @@ class Config(ctypes.Structure):
 
 class Stats(ctypes.Structure):
     _fields_ = [("steps", ctypes.c_uint64), ("pairs", ctypes.c_uint64), ("word_count_actual", ctypes.c_uint64),
-                ("final_alpha", ctypes.c_float), ("pad_", ctypes.c_float)]
+                ("final_alpha", ctypes.c_float), ("pad_", ctypes.c_float), ("train_seconds", ctypes.c_double)]
 
 
 _lib = None
@@ -164,7 +164,7 @@ def train(corpus, counts, d=16, window=5, negative=5, iter=1, workers=1, threads
     if rc != 0:
         raise RuntimeError("oracle_train rejected its configuration")
     return wih, woh, {"steps": st.steps, "pairs": st.pairs, "word_count_actual": st.word_count_actual,
-                      "final_alpha": st.final_alpha}
+                      "final_alpha": st.final_alpha, "train_seconds": st.train_seconds}
 
 
 def minibatch(inputM, outputM, meta, first, alpha, acc64=False):
