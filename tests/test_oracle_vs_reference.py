@@ -4,9 +4,15 @@ configurations (beyond the fixed golden cases).
 The reference binary (oracle/_ref/dsgl_ref) is compiled from the reference checkout by
 oracle/build_ref.sh where that checkout exists; elsewhere these tests are skipped.  One
 compute thread (-threads 2) makes the reference deterministic; the oracle then must give
-the same vocabulary order and the same Wih and Woh bit for bit.  On a few random inputs the
-reference binary dies with SIGSEGV before it prints anything (3 of 40 seeds tried: set-up
-code of the reference, before training); such a case is skipped, not compared.
+the same vocabulary order and the same Wih and Woh bit for bit.
+
+The reference's model-sync thread (include/dsgl.hpp:641-711) picks one random row per block
+of equal counts and compares it with sync_ind[i - 1] before anything has been pushed when
+the first block (the largest count) holds more than one vertex and the pick is not row 0:
+it reads an empty vector and dies with SIGSEGV.  The harness lets that thread run its
+final round after training, so a corpus whose largest count is shared crashes the
+reference (5 of 40 seeds of this generator, all with exactly that tie).  The generator
+breaks such a tie with one more occurrence of a top vertex.
 """
 import os
 import subprocess
@@ -30,13 +36,17 @@ def random_case(seed):
     for _ in range(int(rng.integers(50, 250))):
         toks.extend(rng.choice(V, size=int(rng.integers(1, 90)), p=w).tolist())
         toks.append(-1)
+    counts = np.bincount([t for t in toks if t >= 0], minlength=V)
+    top = np.flatnonzero(counts == counts.max())
+    if len(top) > 1:  # a shared largest count crashes the reference's sync round (see above)
+        toks.extend([int(top[0]), -1])
     cfg = dict(V=V, d=int(rng.choice([4, 8, 12, 16, 20, 32, 36, 64])), window=int(rng.integers(1, 12)),
                negative=int(rng.integers(0, 11)), iter=int(rng.integers(1, 3)),
                sample=float(rng.choice([0.0, 1e-4, 1e-3, 1e-2])), alpha=float(rng.choice([0.01, 0.025, 0.05])))
     return cfg, np.array(toks, dtype=np.int32)
 
 
-@pytest.mark.parametrize("seed", [101, 202, 303, 404, 1000, 1001, 1002, 1003])
+@pytest.mark.parametrize("seed", [19, 26, 101, 202, 303, 404, 1000, 1001, 1002, 1003])
 def test_oracle_equals_reference_on_random_configs(seed, oracle_mod):
     cfg, corpus = random_case(seed)
     V, d = cfg["V"], cfg["d"]
@@ -48,9 +58,7 @@ def test_oracle_equals_reference_on_random_configs(seed, oracle_mod):
                  "-iter", str(cfg["iter"]), "-sample", repr(cfg["sample"]), "-alpha", repr(cfg["alpha"]),
                  "-threads", "2", "-debug", "0", "-eoutput", pre + ".txt"]  # the reference always saves
         r = subprocess.run([REF_BIN, cpath, str(V), pre] + flags, capture_output=True, text=True, timeout=600)
-        if r.returncode < 0:  # the reference itself dies on some inputs (see the module docstring)
-            pytest.skip("the reference was killed by signal %d on this configuration" % -r.returncode)
-        assert r.returncode == 0, r.stderr[-2000:]
+        assert r.returncode == 0, (r.returncode, r.stderr[-2000:])
         rwih = np.fromfile(pre + ".wih", dtype=np.float32).reshape(V, d)
         rwoh = np.fromfile(pre + ".woh", dtype=np.float32).reshape(V, d)
         rorder = np.fromfile(pre + ".order", dtype=np.uint32)
