@@ -13,6 +13,7 @@ import numpy as np
 import pytest
 
 import sgns
+from random_configs import random_case
 
 pytestmark = pytest.mark.gpu
 
@@ -242,27 +243,10 @@ def test_pinned_host_corpus_is_read_in_place(sgns_lib):
         assert e.value.status == sgns.EINVAL
 
 
-def random_config(seed):
-    """A random configuration and power-law corpus (the generator of the oracle's
-    differential test against the reference)."""
-    rng = np.random.default_rng(seed)
-    V = int(rng.integers(1001, 2500))
-    w = (np.arange(V) + rng.uniform(2, 30)) ** -rng.uniform(0.6, 1.2)
-    w /= w.sum()
-    toks = []
-    for _ in range(int(rng.integers(50, 250))):
-        toks.extend(rng.choice(V, size=int(rng.integers(1, 90)), p=w).tolist())
-        toks.append(-1)
-    cfg = dict(V=V, d=int(rng.choice([4, 8, 12, 16, 20, 32, 36, 64])), window=int(rng.integers(1, 12)),
-               negative=int(rng.integers(0, 11)), iter=int(rng.integers(1, 3)),
-               sample=float(rng.choice([0.0, 1e-4, 1e-3, 1e-2])), alpha=float(rng.choice([0.01, 0.025, 0.05])))
-    return cfg, np.array(toks, dtype=np.int32)
-
-
 @pytest.mark.parametrize("seed", [101, 303, 1002, 1003, 2054, 2192])
 @pytest.mark.parametrize("engine,storage", [("plain", "fp32"), ("persistent", "fp32"), ("persistent", "bf16")])
 def test_engines_match_oracle_on_random_configs(seed, engine, storage, sgns_lib, oracle_mod):
-    cfg, corpus = random_config(seed)
+    cfg, corpus = random_case(seed)
     wih, woh, st, _ = gpu_train(cfg, corpus, engine, storage, workers=0, wpc=0, mode="exact")
     policy = oracle_mod.POLICY_REF if engine == "plain" else oracle_mod.POLICY_WINDOW
     owih, owoh, ost = oracle_train(oracle_mod, cfg, corpus, policy, storage)

@@ -6,13 +6,8 @@ oracle/build_ref.sh where that checkout exists; elsewhere these tests are skippe
 compute thread (-threads 2) makes the reference deterministic; the oracle then must give
 the same vocabulary order and the same Wih and Woh bit for bit.
 
-The reference's model-sync thread (include/dsgl.hpp:641-711) picks one random row per block
-of equal counts and compares it with sync_ind[i - 1] before anything has been pushed when
-the first block (the largest count) holds more than one vertex and the pick is not row 0:
-it reads an empty vector and dies with SIGSEGV.  The harness lets that thread run its
-final round after training, so a corpus whose largest count is shared crashes the
-reference (5 of 40 seeds of this generator, all with exactly that tie).  The generator
-breaks such a tie with one more occurrence of a top vertex.
+The configurations and corpora come from tests/random_configs.py (which also explains
+why it breaks ties of the largest count: they crash the reference).
 """
 import os
 import subprocess
@@ -21,29 +16,12 @@ import tempfile
 import numpy as np
 import pytest
 
+from random_configs import random_case
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 REF_BIN = os.path.join(ROOT, "oracle", "_ref", "dsgl_ref")
 
 pytestmark = pytest.mark.skipif(not os.path.exists(REF_BIN), reason="reference binary not built here")
-
-
-def random_case(seed):
-    rng = np.random.default_rng(seed)
-    V = int(rng.integers(1001, 2500))  # the reference asserts V > 1000
-    w = (np.arange(V) + rng.uniform(2, 30)) ** -rng.uniform(0.6, 1.2)
-    w /= w.sum()
-    toks = []
-    for _ in range(int(rng.integers(50, 250))):
-        toks.extend(rng.choice(V, size=int(rng.integers(1, 90)), p=w).tolist())
-        toks.append(-1)
-    counts = np.bincount([t for t in toks if t >= 0], minlength=V)
-    top = np.flatnonzero(counts == counts.max())
-    if len(top) > 1:  # a shared largest count crashes the reference's sync round (see above)
-        toks.extend([int(top[0]), -1])
-    cfg = dict(V=V, d=int(rng.choice([4, 8, 12, 16, 20, 32, 36, 64])), window=int(rng.integers(1, 12)),
-               negative=int(rng.integers(0, 11)), iter=int(rng.integers(1, 3)),
-               sample=float(rng.choice([0.0, 1e-4, 1e-3, 1e-2])), alpha=float(rng.choice([0.01, 0.025, 0.05])))
-    return cfg, np.array(toks, dtype=np.int32)
 
 
 @pytest.mark.parametrize("seed", [19, 26, 101, 202, 303, 404, 1000, 1001, 1002, 1003])
