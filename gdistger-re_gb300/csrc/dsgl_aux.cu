@@ -134,6 +134,8 @@ __global__ void max_walk_kernel(const int32_t* rows, int64_t n, int32_t* out) {
   if ((threadIdx.x & 31) == 0 && best > 0) atomicMax(out, best);
 }
 
+// A negative count (rejected by its own minibatch) adds nothing, so no later minibatch's
+// offset points before the start of the caller's row arrays.
 __global__ void prefix_offsets_kernel(const int32_t* cnt_a, const int32_t* cnt_b, int n, int64_t* off_a,
                                       int64_t* off_b) {
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -141,8 +143,8 @@ __global__ void prefix_offsets_kernel(const int32_t* cnt_a, const int32_t* cnt_b
     for (int i = 0; i < n; i++) {
       off_a[i] = a;
       off_b[i] = bb;
-      a += cnt_a[i];
-      bb += cnt_b[i];
+      a += cnt_a[i] > 0 ? cnt_a[i] : 0;
+      bb += cnt_b[i] > 0 ? cnt_b[i] : 0;
     }
   }
 }
