@@ -20,6 +20,16 @@ def test_every_declared_symbol_is_exported(sgns_lib):
 
 
 
+
+@pytest.mark.parametrize("cmd", [["gcc", "-std=c99", "-x", "c"], ["g++", "-std=c++11", "-x", "c++"]])
+def test_header_compiles_alone(cmd, tmp_path):
+    """include/sgns.h is self-contained and warning-free as C99 and as C++11, the languages
+    of the callers it replaces (the reference builds its trainer as C++)."""
+    src = tmp_path / "inc.txt"
+    src.write_text('#include "sgns.h"\n')
+    subprocess.run(cmd + ["-pedantic", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I",
+                          os.path.dirname(sgns.HEADER), str(src)], check=True)
+
 @pytest.mark.parametrize("ctype,cname", [(sgns.Options, "sgns_options"), (sgns.Stats, "sgns_stats")])
 def test_ctypes_structs_match_the_header(ctype, cname, tmp_path):
     """The binding's struct mirrors have the C layout of include/sgns.h: size and the
