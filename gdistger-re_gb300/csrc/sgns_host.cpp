@@ -950,12 +950,13 @@ sgns_status sgns_train(sgns_handle* h) {
   } else {
     // Default worker count.  Each worker of the reference policy holds snapshots of about
     // max(len1,len2)*K negative rows and two walks' rows and writes them back over the
-    // tables; once all workers together hold a sizeable fraction of the V rows, those
-    // write-backs erase each other's updates (link-prediction AUC on a 100k-vertex SBM:
-    // 0.795 at 152 workers, 0.60 at 304, 0.50 at 608).  V / 700 workers keep that
-    // fraction near 0.3.
+    // tables; with many workers in flight those write-backs erase each other's updates.
+    // Link-prediction AUC on 4-block SBMs (10% holdout): at 100k vertices 0.795 with 152
+    // workers, 0.60 with 304, 0.50 with 608 (GB300); at 1.1M vertices 0.708 with 1571
+    // (GB300), and with every worker in flight at once on the host (the same policy run
+    // step by step round-robin) 0.717 with 1571 and 0.783 with 785.  V / 1400 workers.
     workers = h->opt.workers > 0 ? h->opt.workers
-                                 : (int)std::max<int64_t>(1, std::min<int64_t>(h->num_sms * 16, h->V / 700));
+                                 : (int)std::max<int64_t>(1, std::min<int64_t>(h->num_sms * 16, h->V / 1400));
     const size_t stride = plain_worker_bytes(h->opt.size, h->opt.window, h->opt.negative, h->lmax);
     const size_t budget = (size_t)8 << 30;  // HBM set aside for per-worker buffers
     if (h->opt.workers == 0 && stride * (size_t)workers > budget) workers = std::max<int>(1, (int)(budget / stride));
