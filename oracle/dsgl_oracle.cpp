@@ -616,7 +616,26 @@ struct Worker {
 };
 
 template <int S>
-void run_workers(Shared& sh, typename Store<S>::T* Wih, typename Store<S>::T* Woh, int threads) {
+void run_workers(Shared& sh, typename Store<S>::T* Wih, typename Store<S>::T* Woh, int threads, int schedule) {
+  if (schedule == 1) {
+    // every worker in flight: thread t owns workers t, t + threads, ... and gives each of
+    // them one step in turn until all have finished their slices
+#pragma omp parallel num_threads(threads < 1 ? 1 : threads)
+    {
+      const int nt = omp_get_num_threads(), t = omp_get_thread_num();
+      std::vector<Worker<S>*> mine;
+      for (int id = t; id < sh.workers; id += nt) mine.push_back(new Worker<S>(sh, Wih, Woh, (uint32_t)id));
+      size_t live = mine.size();
+      while (live)
+        for (auto& w : mine)
+          if (w && !w->iterate()) {
+            delete w;
+            w = nullptr;
+            live--;
+          }
+    }
+    return;
+  }
   if (sh.workers == 1 || threads <= 1) {
     // deterministic: workers run one after another, each to completion
     for (int id = 0; id < sh.workers; id++) {
@@ -645,7 +664,10 @@ struct oracle_config {
   int32_t table_threads;  // -threads of the reference: partition of the table reduction
   int32_t policy;         // 0 = reference buffers, 1 = GPU window/direct policy
   int32_t storage;        // 0 = f32, 1 = bf16 + stochastic rounding, 2 = f64
-  int32_t pad_;
+  int32_t schedule;       // 0 = each worker runs to completion (at most `threads` in
+                          // flight, as the reference's compute threads); 1 = every worker in
+                          // flight at once, each thread stepping its workers round-robin
+                          // (how a GPU runs them; used to study concurrency, not for parity)
   int64_t table_size;
   float sample, alpha;
   uint64_t sr_seed;
@@ -723,11 +745,11 @@ int oracle_train(const oracle_config* cfg, const int32_t* counts, int64_t V, con
   sh.pairs = 0;
   const double t0 = omp_get_wtime();
   if (cfg->storage == STORE_F32)
-    run_workers<STORE_F32>(sh, (float*)Wih, (float*)Woh, cfg->threads);
+    run_workers<STORE_F32>(sh, (float*)Wih, (float*)Woh, cfg->threads, cfg->schedule);
   else if (cfg->storage == STORE_BF16)
-    run_workers<STORE_BF16>(sh, (uint16_t*)Wih, (uint16_t*)Woh, cfg->threads);
+    run_workers<STORE_BF16>(sh, (uint16_t*)Wih, (uint16_t*)Woh, cfg->threads, cfg->schedule);
   else if (cfg->storage == STORE_F64)
-    run_workers<STORE_F64>(sh, (double*)Wih, (double*)Woh, cfg->threads);
+    run_workers<STORE_F64>(sh, (double*)Wih, (double*)Woh, cfg->threads, cfg->schedule);
   else
     return -1;
   if (stats) {

@@ -20,7 +20,7 @@ class Config(ctypes.Structure):
     _fields_ = [("d", ctypes.c_int32), ("window", ctypes.c_int32), ("negative", ctypes.c_int32),
                 ("iter", ctypes.c_int32), ("workers", ctypes.c_int32), ("threads", ctypes.c_int32),
                 ("table_threads", ctypes.c_int32), ("policy", ctypes.c_int32), ("storage", ctypes.c_int32),
-                ("pad_", ctypes.c_int32), ("table_size", ctypes.c_int64), ("sample", ctypes.c_float),
+                ("schedule", ctypes.c_int32), ("table_size", ctypes.c_int64), ("sample", ctypes.c_float),
                 ("alpha", ctypes.c_float), ("sr_seed", ctypes.c_uint64)]
 
 
@@ -139,11 +139,13 @@ def init_wih(V, d):
 
 def train(corpus, counts, d=16, window=5, negative=5, iter=1, workers=1, threads=1, table_threads=12,
           policy=POLICY_REF, storage=STORE_F32, table_size=100000000, sample=1e-3, alpha=0.025,
-          sr_seed=0x5EED):
+          sr_seed=0x5EED, schedule=0):
     """Runs the restated trainer; returns (Wih, Woh, stats) in sorted-row order.
 
     Wih starts from the reference initialisation (bf16: rounded to nearest even),
     Woh from zeros.  workers > 1 with threads == 1 runs the workers one after another.
+    schedule=1 keeps every worker in flight at once (each thread steps its workers
+    round-robin), as a GPU runs them: a model of concurrency, not a parity mode.
     """
     corpus = np.ascontiguousarray(corpus, dtype=np.int32)
     counts = np.ascontiguousarray(counts, dtype=np.int32)
@@ -157,7 +159,7 @@ def train(corpus, counts, d=16, window=5, negative=5, iter=1, workers=1, threads
         wih, woh = w0.astype(np.float64), np.zeros((V, d), np.float64)
     cfg = Config(d=d, window=window, negative=negative, iter=iter, workers=workers, threads=threads,
                  table_threads=table_threads, policy=policy, storage=storage, table_size=table_size,
-                 sample=sample, alpha=alpha, sr_seed=sr_seed)
+                 sample=sample, alpha=alpha, sr_seed=sr_seed, schedule=schedule)
     st = Stats()
     rc = lib().oracle_train(ctypes.byref(cfg), _p(counts), V, _p(corpus), len(corpus), _p(wih), _p(woh),
                             ctypes.byref(st))

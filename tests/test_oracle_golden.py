@@ -114,3 +114,19 @@ def test_embedding_writer_reproduces_reference_file(name, sgns_lib, oracle_mod, 
         assert raw[pos:pos + len(ident)] == ident
         row = np.frombuffer(raw[pos + len(ident):pos + len(ident) + 4 * d], np.float32)
         assert np.array_equal(row.view(np.uint32), wih[r].view(np.uint32))
+
+
+@pytest.mark.parametrize("policy", [0, 1])
+def test_round_robin_schedule_keeps_the_control_flow(policy, oracle_mod):
+    """The schedule that keeps every worker in flight (the oracle's model of a GPU's
+    concurrency) trains the same steps, pairs and words as workers run to completion."""
+    meta, corpus, _ = load("d128_w10")
+    counts = np.bincount(corpus[corpus >= 0], minlength=meta["V"]).astype(np.int32)
+    runs = []
+    for schedule, threads in ((0, 1), (1, 1), (1, 3)):
+        _, _, st = oracle_mod.train(corpus, counts, d=8, window=meta["window"], negative=meta["negative"],
+                                    iter=meta["iter"], workers=17, threads=threads, table_threads=meta["table_threads"],
+                                    policy=policy, storage=oracle_mod.STORE_F32, table_size=meta["table_size"],
+                                    sample=meta["sample"], alpha=meta["alpha"], schedule=schedule)
+        runs.append((st["steps"], st["pairs"], st["word_count_actual"]))
+    assert runs[0][0] > 0 and runs[0] == runs[1] == runs[2], runs
