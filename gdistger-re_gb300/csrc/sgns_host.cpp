@@ -351,6 +351,13 @@ sgns_status persistent_shape(sgns_handle* h, int wpc, int* workers) {
     return fail(h, SGNS_EINVAL, "a %d-warp CTA does not fit in shared memory (d=%d, walks up to %d)", wpc,
                 o.size, h->lmax);
   *workers = ctas * wpc * h->num_sms;
+  // At most V/400 workers: with many workers per vertex in flight, hot rows are updated
+  // from many stale window copies at once, which costs link-prediction quality (4-block
+  // SBM, 100k vertices, every worker in flight: AUC 0.7865 with 266 workers, 0.7842 with
+  // 532, 0.7804 with 1064, against the reference trainer's 0.7886).  Large vocabularies
+  // keep the full resident count (2.24M vertices: 5596 > 1064).
+  const int64_t cap = std::max<int64_t>(1, h->V / 400);
+  if (*workers > cap) *workers = (int)cap;
   return SGNS_OK;
 }
 
