@@ -251,12 +251,14 @@ def _train_embedding(sgns, counts, corpus_np, V, engine, storage, device, pos=No
 
 
 def run_auc(args):
-    print(json.dumps(auc_suite(args.auc_vertices, cpu=not args.auc_skip_cpu)), flush=True)
+    print(json.dumps(auc_suite(args.auc_vertices, cpu=not args.auc_skip_cpu, persistent_workers=args.auc_workers,
+                               plain_workers=args.auc_plain_workers)), flush=True)
 
 
-def auc_suite(V, cpu=True):
+def auc_suite(V, cpu=True, persistent_workers=0, plain_workers=0):
     """SBM graph with a 10% holdout, information-oriented walks (lengths 21-80, mean ~40);
-    the same corpus trained by every engine and (cpu=True) by the CPU reference restatement."""
+    the same corpus trained by every engine and (cpu=True) by the CPU reference restatement.
+    persistent_workers / plain_workers: worker counts (0 = each engine's default)."""
     import torch
     import sgns
     import synth
@@ -276,7 +278,8 @@ def auc_suite(V, cpu=True):
            "tokens": int(len(c)), "train": {**TRAIN, "iter": 1}}
     for name, eng, sto in (("gpu_plain_fp32", "plain", "fp32"), ("gpu_persistent_fp32", "persistent", "fp32"),
                            ("gpu_persistent_bf16", "persistent", "bf16")):
-        emb, st, auc = _train_embedding(sgns, counts, c, V, eng, sto, 0, pos, neg)
+        emb, st, auc = _train_embedding(sgns, counts, c, V, eng, sto, 0, pos, neg,
+                                        workers=plain_workers if eng == "plain" else persistent_workers)
         out[name] = {"auc": auc, "pairs_per_s": st.pairs / st.train_ms * 1e3,
                      "workers": st.workers}
     if cpu:
@@ -657,6 +660,8 @@ def main():
     ap.add_argument("--auc", action="store_true", help="link-prediction AUC of every engine and the CPU reference")
     ap.add_argument("--auc-vertices", type=int, default=100000)
     ap.add_argument("--auc-skip-cpu", action="store_true")
+    ap.add_argument("--auc-workers", type=int, default=0, help="persistent-engine workers in --auc (0 = default)")
+    ap.add_argument("--auc-plain-workers", type=int, default=0, help="plain-engine workers in --auc (0 = default)")
     ap.add_argument("--mb-error", action="store_true", help="bf16 per-minibatch error against fp64")
     ap.add_argument("--sweep", action="store_true", help="d x K x storage sweep, persistent vs plain")
     ap.add_argument("--adjoint", action="store_true", help="loss + adjoint throughput (row-gradient GB/s)")
