@@ -234,6 +234,16 @@ def run_reference(args, wl):
 # evaluation modes (not the headline line): link-prediction AUC across engines and the
 # CPU reference, bf16 per-minibatch error against fp64, the shape sweep, the adjoint.
 
+def _row_roofline(st):
+    """Row-traffic rate of one training call (sgns_stats.row_bytes over its CUDA-event time)
+    against the measured HBM copy bandwidth."""
+    pk = peaks()
+    peak = pk["hbm_gbs"] if pk else 6800.0
+    gbs = st.row_bytes / (st.train_ms / 1e3) / 1e9 if st.train_ms > 0 else 0.0
+    return {"achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+            "peak_source": "measured" if pk else "fallback"}
+
+
 def _train_embedding(sgns, counts, corpus_np, V, engine, storage, device, pos=None, neg=None, **kw):
     """Trains one engine; returns (embedding in vertex order, stats, AUC scored on the GPU
     by sgns_link_scores when pos/neg are given)."""
@@ -281,7 +291,7 @@ def auc_suite(V, cpu=True, persistent_workers=0, plain_workers=0):
         emb, st, auc = _train_embedding(sgns, counts, c, V, eng, sto, 0, pos, neg,
                                         workers=plain_workers if eng == "plain" else persistent_workers)
         out[name] = {"auc": auc, "pairs_per_s": st.pairs / st.train_ms * 1e3,
-                     "workers": st.workers}
+                     "workers": st.workers, "roofline": _row_roofline(st)}
     if cpu:
         cores = os.cpu_count() or 1
         wih, _, st = oracle.train(c, counts, d=TRAIN["size"], window=TRAIN["window"], negative=TRAIN["negative"],
@@ -447,7 +457,8 @@ def run_sweep(args):
                     ps = t.train()
                 rows.append({"d": d, "K": K, "storage": sto, "persistent_pairs_per_s": st.pairs / st.train_ms * 1e3,
                              "warps_per_cta": st.warps_per_cta, "workers": st.workers,
-                             "plain_pairs_per_s": ps.pairs / ps.train_ms * 1e3,
+                             "persistent_roofline": _row_roofline(st),
+                             "plain_pairs_per_s": ps.pairs / ps.train_ms * 1e3, "plain_roofline": _row_roofline(ps),
                              "speedup": (st.pairs / st.train_ms) / (ps.pairs / ps.train_ms)})
                 print(json.dumps(rows[-1]), flush=True)
     print(json.dumps({"mode": "sweep", "graph": "Chung-Lu V=%d E=%d" % (wl["V"], ix.numel() // 2),
