@@ -37,7 +37,8 @@ def test_full_size_control_flow_equals_the_oracle(sgns_lib, oracle_mod):
         wih = t.embeddings(0)
     assert np.isfinite(wih).all() and float(np.abs(wih).max()) > 0
     _, _, ost = oracle_mod.train(c, counts, d=4, window=tr["window"], negative=tr["negative"], iter=1,
-                                 workers=st.workers, threads=os.cpu_count() or 1, table_threads=tr["threads"],
+                                 workers=st.workers, threads=len(os.sched_getaffinity(0)),
+                                 table_threads=tr["threads"],
                                  policy=oracle_mod.POLICY_WINDOW, storage=oracle_mod.STORE_F32,
                                  table_size=tr["table_size"], sample=tr["sample"], alpha=tr["alpha"])
     assert st.word_count_actual == len(c)
