@@ -51,6 +51,14 @@ WORKLOADS = {
 TRAIN = dict(size=128, window=10, negative=5, sample=1e-3, alpha=0.01, table_size=100_000_000, threads=12)
 
 
+def host_cores():
+    """Host cores this process may run on (its CPU affinity), the thread count of the CPU legs."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
 def peaks():
     try:
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -133,7 +141,7 @@ def cpu_baseline(corpus_host, V, seconds_hint=10.0, tokens=None):
     leaves out its set-up (vocabulary, unigram table, initialisation)."""
     import oracle
 
-    cores = os.cpu_count() or 1
+    cores = host_cores()
     if tokens is None:
         # about 30k tokens per second per host core (x86 and Grace alike): seconds_hint of training
         tokens = int(max(200_000, min(len(corpus_host), cores * 30_000 * seconds_hint)))
@@ -188,7 +196,7 @@ def run_reference(args, wl):
 
     ip, ix = synth.chung_lu(wl["V"], wl["E"], wl["gamma"], seed=2024, device="cpu")
     tr_ip, tr_ix, _, _ = synth.holdout(ip, ix, 0.1, seed=7)
-    cores = os.cpu_count() or 1
+    cores = host_cores()
     # walks of a vertex subset are enough for a bounded sample per step
     nw = min(wl["V"] * wl["walks"], max(20000, cores * 2500))
     starts_graph = (tr_ip, tr_ix)
@@ -293,7 +301,7 @@ def auc_suite(V, cpu=True, persistent_workers=0, plain_workers=0):
         out[name] = {"auc": auc, "pairs_per_s": st.pairs / st.train_ms * 1e3,
                      "workers": st.workers, "roofline": _row_roofline(st)}
     if cpu:
-        cores = os.cpu_count() or 1
+        cores = host_cores()
         wih, _, st = oracle.train(c, counts, d=TRAIN["size"], window=TRAIN["window"], negative=TRAIN["negative"],
                                   iter=1, workers=cores, threads=cores, table_threads=TRAIN["threads"],
                                   policy=oracle.POLICY_REF, storage=oracle.STORE_F32, table_size=TRAIN["table_size"],
