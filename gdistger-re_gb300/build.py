@@ -16,7 +16,7 @@ ROOT = os.path.dirname(HERE)
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["dsgl_window.cu", "dsgl_plain.cu", "dsgl_aux.cu", "dsgl_adjoint.cu", "dsgl_noalloc.cu",
-              "dsgl_ingest.cu", "dsgl_eval.cu"]
+              "dsgl_ingest.cu", "dsgl_eval.cu", "dsgl_walk.cu"]
 CPP_SOURCES = ["sgns_host.cpp"]
 LIB = os.path.join(OUT, "libsgns.so")
 CLI = os.path.join(OUT, "sgns_train")
@@ -56,7 +56,10 @@ def build(verbose_ptxas=False, force=False):
         o = os.path.join(OUT, src + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append([NVCC, "-O2", "-std=c++17", "-Xcompiler", "-fPIC,-Wall", "-I", os.path.join(ROOT, "include"),
+            # -ffp-contract=off: host float expressions (vocabulary tables, the walker's
+            # entropy table) evaluate as written, with no fused multiply-add, on every host
+            jobs.append([NVCC, "-O2", "-std=c++17", "-Xcompiler", "-fPIC,-Wall,-ffp-contract=off",
+                         "-I", os.path.join(ROOT, "include"),
                          "-c", s, "-o", o])
     logs = []
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:

@@ -247,6 +247,30 @@ sgns_status write_embedding(const uint32_t* order, const float* w, int64_t V, in
   return ok ? SGNS_OK : SGNS_EIO;
 }
 
+// x * log2(x) for integers 0..n-1 from basic IEEE operations only (the same bits on every
+// host): log2 x = e + ln(m) log2(e) for x = 2^e m, m in [1, 2), ln(m) = 2 atanh(s) with
+// s = (m - 1) / (m + 1) by its odd series to s^39.
+void xlog2x_table(int n, double* t) {
+  for (int x = 0; x < n; x++) {
+    if (x == 0) {
+      t[x] = 0.0;
+      continue;
+    }
+    int e = 0;
+    while ((x >> (e + 1)) != 0) e++;
+    uint64_t bits = (uint64_t)(1023 + e) << 52;
+    double p2;
+    memcpy(&p2, &bits, 8);
+    const double m = (double)x / p2;
+    const double s = (m - 1.0) / (m + 1.0);
+    const double s2 = s * s;
+    double sum = 0.0;
+    for (int k = 39; k >= 1; k -= 2) sum = sum * s2 + 1.0 / (double)k;
+    const double ln_m = 2.0 * (s * sum);
+    t[x] = (double)x * ((double)e + ln_m * 1.4426950408889634);
+  }
+}
+
 void build_exp_table(float* t) {  // dsgl.hpp:1557-1562
   for (int i = 0; i < kExpTableSize + 1; i++) {
     const float e = expf(((float)i / (float)kExpTableSize * 2 - 1) * kMaxExp);
@@ -448,8 +472,9 @@ std::string tune_key(const sgns_handle* h) {
   cudaDeviceProp prop{};
   if (cudaGetDeviceProperties(&prop, h->opt.device) != cudaSuccess) prop.name[0] = 0;
   char key[384];
-  snprintf(key, sizeof key, "%s|sms=%d|d=%d|w=%d|K=%d|storage=%d|lmax=%d|workers=%d", prop.name, h->num_sms,
-           h->opt.size, h->opt.window, h->opt.negative, h->opt.storage, h->lmax, h->opt.workers);
+  // V enters the key because the default worker count is capped at V/400
+  snprintf(key, sizeof key, "%s|sms=%d|d=%d|w=%d|K=%d|storage=%d|lmax=%d|workers=%d|V=%lld", prop.name, h->num_sms,
+           h->opt.size, h->opt.window, h->opt.negative, h->opt.storage, h->lmax, h->opt.workers, (long long)h->V);
   for (char* c = key; *c; c++)
     if (*c == '\t' || *c == '\n') *c = ' ';
   return key;
@@ -636,6 +661,9 @@ int report_error(int status, const char* fmt, ...) {
   vsnprintf(buf, sizeof buf, fmt, ap);
   va_end(ap);
   g_create_err = buf;
+  // as in fail(): a failed runtime call also left the per-thread last error set, which the
+  // next launcher would otherwise read back as its own failure
+  if (status == SGNS_ECUDA || status == SGNS_ENOMEM) cudaGetLastError();
   return status;
 }
 }  // namespace sgns
@@ -669,6 +697,9 @@ int32_t sgns_internal_write_embedding(const uint32_t* order, const float* w, int
   if (!order || !w || !path || V < 0 || d < 1) return SGNS_EINVAL;
   return write_embedding(order, w, V, d, binary != 0, path);
 }
+
+// The walker's x * log2(x) table as sgns_info_walks uploads it; exported for the CPU tests.
+void sgns_internal_xlog2x_table(int32_t n, double* t) { xlog2x_table(n, t); }
 
 void sgns_default_options(sgns_options* o) {
   std::memset(o, 0, sizeof *o);
@@ -1265,6 +1296,106 @@ sgns_status sgns_link_scores(int32_t dtype, int32_t d, const void* table, int64_
       (e = cudaStreamSynchronize(s)) != cudaSuccess)
     return fail(nullptr, SGNS_ECUDA, "link scores: %s", cudaGetErrorString(e));
   if (hb) return fail(nullptr, SGNS_EINVAL, "a pair names a row outside [0, %lld)", (long long)V);
+  return SGNS_OK;
+}
+
+namespace {
+// Checks a device CSR graph; status word in scratch.  Returns SGNS_OK or the error.
+sgns_status check_csr(const char* what, const int64_t* indptr, const int32_t* indices, int64_t V, int64_t E,
+                      int32_t* status, int sms, cudaStream_t s) {
+  int32_t hs = 0;
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(status, 0, sizeof(int32_t), s)) != cudaSuccess ||
+      (e = launch_validate_csr(indptr, indices, V, E, status, sms, s)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(&hs, status, sizeof hs, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    return fail(nullptr, SGNS_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+  if (hs & 4) return fail(nullptr, SGNS_EINVAL, "%s: indptr must start at 0, end at n_edges and not decrease", what);
+  if (hs & 1) return fail(nullptr, SGNS_EINVAL, "%s: a neighbour id lies outside [0, %lld)", what, (long long)V);
+  return SGNS_OK;
+}
+
+int device_sms() {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return 0;
+  return sms;
+}
+}  // namespace
+
+sgns_status sgns_edge_common_neighbors(const int64_t* indptr, const int32_t* indices, int64_t V, int64_t n_edges,
+                                       int32_t* cn, void* stream) {
+  NvtxRange r_("sgns_edge_common_neighbors");
+  if (V < 1 || V > INT32_MAX || n_edges < 0 || !indptr || (n_edges > 0 && (!indices || !cn)))
+    return fail(nullptr, SGNS_EINVAL, "bad common-neighbour arguments");
+  const int sms = device_sms();
+  if (!sms) return fail(nullptr, SGNS_ECUDA, "no current CUDA device");
+  DeviceScratch* ds = device_scratch();
+  if (!ds) return fail(nullptr, SGNS_ECUDA, "no current CUDA device");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  std::lock_guard<std::mutex> g(ds->mx);
+  sgns_status st = ds->ensure(64);
+  if (st) return st;
+  int32_t* status = static_cast<int32_t*>(ds->buf);
+  if ((st = check_csr("common neighbours", indptr, indices, V, n_edges, status, sms, s))) return st;
+  int32_t hs = 0;
+  cudaError_t e;
+  if ((e = launch_edge_common_neighbors(indptr, indices, V, n_edges, cn, status, sms, s)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(&hs, status, sizeof hs, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    return fail(nullptr, SGNS_ECUDA, "common neighbours: %s", cudaGetErrorString(e));
+  if (hs & 2) return fail(nullptr, SGNS_EINVAL, "common neighbours: an adjacency list is not strictly increasing");
+  return SGNS_OK;
+}
+
+sgns_status sgns_info_walks(const sgns_walk_options* o, const int64_t* indptr, const int32_t* indices,
+                            const int32_t* cn, int64_t V, int64_t n_edges, int32_t* corpus, int64_t cap,
+                            int64_t* n_tokens, void* stream) {
+  NvtxRange r_("sgns_info_walks");
+  if (!o || !n_tokens || V < 1 || V > INT32_MAX || n_edges < 0 || !indptr || (n_edges > 0 && (!indices || !cn)) ||
+      cap < 0 || (cap > 0 && !corpus))
+    return fail(nullptr, SGNS_EINVAL, "bad walk arguments");
+  if (o->walker_num < 0 || o->min_length < 0 || o->max_length < 1 || o->max_length > kWalkMaxLength ||
+      !(o->r_threshold == o->r_threshold))
+    return fail(nullptr, SGNS_EINVAL, "walk options: walker_num >= 0, min_length >= 0, max_length in [1, %d]",
+                kWalkMaxLength);
+  *n_tokens = 0;
+  if (o->walker_num == 0) return SGNS_OK;
+  const int sms = device_sms();
+  if (!sms) return fail(nullptr, SGNS_ECUDA, "no current CUDA device");
+  DeviceScratch* ds = device_scratch();
+  if (!ds) return fail(nullptr, SGNS_ECUDA, "no current CUDA device");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  std::lock_guard<std::mutex> g(ds->mx);
+  const size_t xl_bytes = sizeof(double) * (size_t)(kWalkMaxLength + 2);
+  sgns_status st = ds->ensure(256 + xl_bytes + walk_scratch_bytes(o->walker_num));
+  if (st) return st;
+  char* base = static_cast<char*>(ds->buf);
+  int32_t* status = reinterpret_cast<int32_t*>(base);
+  double* xl = reinterpret_cast<double*>(base + 256);
+  void* scratch = base + 256 + xl_bytes;
+  if ((st = check_csr("walks", indptr, indices, V, n_edges, status, sms, s))) return st;
+  std::vector<double> hxl(kWalkMaxLength + 2);
+  xlog2x_table(kWalkMaxLength + 2, hxl.data());
+  int64_t* offsets = nullptr;
+  int64_t total = 0;
+  cudaError_t e;
+  if ((e = cudaMemcpyAsync(xl, hxl.data(), xl_bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+      (e = launch_info_walks_count(indptr, indices, cn, xl, V, o->walker_num, o->min_length, o->max_length,
+                                   o->r_threshold, o->seed, scratch, sms, &offsets, s)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(&total, offsets + o->walker_num, sizeof total, cudaMemcpyDeviceToHost, s)) !=
+          cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    return fail(nullptr, SGNS_ECUDA, "walks: %s", cudaGetErrorString(e));
+  *n_tokens = total;
+  if (total > cap) {
+    if (cap == 0 && !corpus) return SGNS_OK;
+    return fail(nullptr, SGNS_EINVAL, "walks yield %lld tokens, capacity %lld", (long long)total, (long long)cap);
+  }
+  if ((e = launch_info_walks_emit(indptr, indices, cn, xl, V, o->walker_num, o->min_length, o->max_length,
+                                  o->r_threshold, o->seed, offsets, corpus, sms, s)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    return fail(nullptr, SGNS_ECUDA, "walks: %s", cudaGetErrorString(e));
   return SGNS_OK;
 }
 

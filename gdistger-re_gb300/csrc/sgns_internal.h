@@ -188,6 +188,23 @@ cudaError_t launch_vertex_count(const int32_t* tokens, int64_t n, int32_t* count
 cudaError_t launch_link_scores(int storage, const void* table, int d, int64_t V, const int32_t* pairs, int64_t n,
                                float* scores, int32_t* bad, int num_sms, cudaStream_t s);
 
+// information-oriented walks and common-neighbour counts (dsgl_walk.cu)
+constexpr int kWalkMaxLength = 1000;  // vertices per walk (the trainer's limit, dsgl.hpp:23)
+cudaError_t launch_validate_csr(const int64_t* indptr, const int32_t* indices, int64_t V, int64_t E,
+                                int32_t* status, int num_sms, cudaStream_t s);
+cudaError_t launch_edge_common_neighbors(const int64_t* indptr, const int32_t* indices, int64_t V, int64_t E,
+                                         int32_t* cn, int32_t* status, int num_sms, cudaStream_t s);
+int walk_block_threads(int max_length);
+size_t walk_scratch_bytes(int64_t walker_num);
+cudaError_t launch_info_walks_count(const int64_t* indptr, const int32_t* indices, const int32_t* cn,
+                                    const double* xl, int64_t V, int64_t walker_num, int min_length,
+                                    int max_length, double r_threshold, uint64_t seed, void* scratch,
+                                    int num_sms, int64_t** offsets_out, cudaStream_t s);
+cudaError_t launch_info_walks_emit(const int64_t* indptr, const int32_t* indices, const int32_t* cn,
+                                   const double* xl, int64_t V, int64_t walker_num, int min_length, int max_length,
+                                   double r_threshold, uint64_t seed, const int64_t* offsets, int32_t* corpus,
+                                   int num_sms, cudaStream_t s);
+
 void host_exp_table(float* t /* kExpTableSize + 1 */);
 int report_error(int status, const char* fmt, ...);  // sets sgns_last_error(NULL); returns status
 
@@ -212,3 +229,6 @@ extern "C" int32_t sgns_internal_host_vocab(const int32_t* counts, int64_t V, fl
 // w (V x d floats, sorted-row order); exported for the CPU tests.
 extern "C" int32_t sgns_internal_write_embedding(const uint32_t* order, const float* w, int64_t V, int32_t d,
                                                  int32_t binary, const char* path);
+// The walker's x * log2(x) table (n entries) exactly as sgns_info_walks builds it; exported
+// for the CPU tests.
+extern "C" void sgns_internal_xlog2x_table(int32_t n, double* t);

@@ -44,6 +44,11 @@ class Stats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class WalkOptions(ctypes.Structure):
+    _fields_ = [("walker_num", ctypes.c_int64), ("min_length", ctypes.c_int32), ("max_length", ctypes.c_int32),
+                ("r_threshold", ctypes.c_double), ("seed", ctypes.c_uint64)]
+
+
 class SgnsError(RuntimeError):
     def __init__(self, status, msg):
         super().__init__("sgns status %d: %s" % (status, msg))
@@ -94,11 +99,16 @@ def lib():
         L.sgns_link_scores.argtypes = [i32, i32, vp, i64, vp, i64, vp, vp]
         L.sgns_loss_adjoint.argtypes = [i32, i32, i64, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp,
                                         ctypes.POINTER(i64), vp, vp, ctypes.POINTER(i64), vp]
+        L.sgns_edge_common_neighbors.argtypes = [vp, vp, i64, i64, vp, vp]
+        L.sgns_info_walks.argtypes = [ctypes.POINTER(WalkOptions), vp, vp, vp, i64, i64, vp, i64,
+                                      ctypes.POINTER(i64), vp]
         L.sgns_internal_host_vocab.argtypes = [vp, i64, ctypes.c_float, i64, i32, vp, vp, vp, vp,
                                                ctypes.POINTER(ctypes.c_uint64)]
         L.sgns_internal_host_vocab.restype = i32
         L.sgns_internal_write_embedding.argtypes = [vp, vp, i64, i32, i32, ctypes.c_char_p]
         L.sgns_internal_write_embedding.restype = i32
+        L.sgns_internal_xlog2x_table.argtypes = [i32, vp]
+        L.sgns_internal_xlog2x_table.restype = None
         for name in header_functions():  # every declared entry point must be exported
             getattr(L, name)
         _lib = L
@@ -287,6 +297,33 @@ def loss_adjoint(dtype, d, V, in_ptr, in_ids, in_first, out_ptr, out_ids, out_me
     return n_in.value, n_out.value
 
 
+def edge_common_neighbors(indptr, indices, cn, stream=0):
+    """sgns_edge_common_neighbors on device tensors (indptr int64 [V + 1], indices int32 [E],
+    cn int32 [E], filled in place)."""
+    V, E = int(indptr.numel()) - 1, int(indices.numel())
+    _check(lib().sgns_edge_common_neighbors(indptr.data_ptr(), indices.data_ptr() if E else None, V, E,
+                                            cn.data_ptr() if E else None, ctypes.c_void_p(stream)))
+
+
+def info_walks(indptr, indices, cn, walker_num, min_length=20, max_length=80, r_threshold=0.999, seed=1,
+               corpus=None, stream=0):
+    """sgns_info_walks on device tensors.  corpus: int32 device tensor to fill (None: a new
+    one of the exact size, after a counting call).  Returns (corpus, n_tokens)."""
+    import torch
+
+    V, E = int(indptr.numel()) - 1, int(indices.numel())
+    o = WalkOptions(walker_num=int(walker_num), min_length=int(min_length), max_length=int(max_length),
+                    r_threshold=float(r_threshold), seed=int(seed))
+    n = ctypes.c_int64()
+    args = (indptr.data_ptr(), indices.data_ptr() if E else None, cn.data_ptr() if E else None, V, E)
+    if corpus is None:
+        _check(lib().sgns_info_walks(ctypes.byref(o), *args, None, 0, ctypes.byref(n), ctypes.c_void_p(stream)))
+        corpus = torch.empty(max(n.value, 1), dtype=torch.int32, device=indptr.device)
+    _check(lib().sgns_info_walks(ctypes.byref(o), *args, corpus.data_ptr(), int(corpus.numel()), ctypes.byref(n),
+                                 ctypes.c_void_p(stream)))
+    return corpus[:n.value], n.value
+
+
 def host_vocab(counts, sample, table_size, threads):
     """The host set-up sgns_set_vocab performs, run on the CPU without a device: (order of the
     count-sorted rows, unigram table, subsampling keep thresholds, sigmoid table,
@@ -310,3 +347,10 @@ def write_embedding(order, w, path, binary=False):
     w = np.ascontiguousarray(w, dtype=np.float32)
     _check(lib().sgns_internal_write_embedding(_ptr(order), _ptr(w), w.shape[0], w.shape[1], int(binary),
                                                str(path).encode()))
+
+
+def xlog2x_table(n):
+    """The walker's x * log2(x) table as sgns_info_walks builds it (host code, no device)."""
+    t = np.zeros(n, np.float64)
+    lib().sgns_internal_xlog2x_table(n, _ptr(t))
+    return t

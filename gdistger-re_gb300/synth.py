@@ -273,6 +273,124 @@ def information_walks(indptr, indices, walks_per_vertex=10, min_length=20, max_l
     return flat[flat != -2]
 
 
+# ---- platform-independent generators (numpy integer arithmetic only) ----------------
+# The same seed gives the same graph, holdout and pairs on every host (x86 and Arm alike),
+# so a corpus drawn from them on the GPU can be compared with one a CPU trainer used.
+_G = np.uint64(0x9E3779B97F4A7C15)
+
+
+def _mix64(z):
+    """SplitMix64 finaliser (Steele, Lea, Flood 2014) on a uint64 array, adding G first."""
+    with np.errstate(over="ignore"):
+        z = np.asarray(z, dtype=np.uint64) + _G
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+
+def _stream(seed, purpose, n):
+    """n uint64 draws of the stream (seed, purpose)."""
+    with np.errstate(over="ignore"):
+        base = _mix64(np.uint64(seed) ^ (np.uint64(purpose) * _G))
+        return _mix64(base + np.arange(n, dtype=np.uint64) * _G)
+
+
+def _below(r, n):
+    """Lemire's multiply-shift: uniform integers in [0, n) from 64-bit draws (high 32 bits)."""
+    return ((r >> np.uint64(32)) * np.uint64(n)) >> np.uint64(32)
+
+
+def _csr_from_pairs_np(a, b, V):
+    """Undirected simple graph from pairs: no self loops, no duplicates, sorted lists."""
+    keep = a != b
+    a, b = a[keep], b[keep]
+    lo, hi = np.minimum(a, b).astype(np.int64), np.maximum(a, b).astype(np.int64)
+    key = np.unique(lo * V + hi)
+    lo, hi = key // V, key % V
+    u = np.concatenate([lo, hi])
+    v = np.concatenate([hi, lo])
+    order = np.argsort(u * V + v, kind="stable")
+    u, v = u[order], v[order]
+    indptr = np.zeros(V + 1, np.int64)
+    np.cumsum(np.bincount(u, minlength=V), out=indptr[1:])
+    return indptr, v.astype(np.int32)
+
+
+def sbm_csr(V, E, blocks=4, ratio=20.0, seed=1):
+    """k equal blocks of consecutive vertex ids; a candidate edge lies within a block with
+    the probability the p_in / p_out ratio gives for equal blocks.  About E undirected
+    edges (duplicates and self pairs of the int(1.05 E) candidates are dropped).
+    Returns (indptr int64 [V + 1], indices int32, block_of int32 [V])."""
+    bs = V // blocks
+    block_of = np.minimum(np.arange(V) // bs, blocks - 1).astype(np.int32)
+    within = blocks * bs * bs / 2.0
+    between = blocks * (blocks - 1) / 2.0 * bs * bs
+    p_within = ratio * within / (ratio * within + between)
+    n = int(E * 1.05) + 16
+    thr = np.uint64(int(p_within * 2.0 ** 53))
+    inside = (_stream(seed, 1, n) >> np.uint64(11)) < thr
+    b1 = _below(_stream(seed, 2, n), blocks).astype(np.int64)
+    off = 1 + _below(_stream(seed, 3, n), blocks - 1).astype(np.int64)
+    b2 = np.where(inside, b1, (b1 + off) % blocks)
+    u = b1 * bs + _below(_stream(seed, 4, n), bs).astype(np.int64)
+    v = b2 * bs + _below(_stream(seed, 5, n), bs).astype(np.int64)
+    indptr, indices = _csr_from_pairs_np(u, v, V)
+    return indptr, indices, block_of
+
+
+def holdout_csr(indptr, indices, frac=0.1, seed=7):
+    """The link-prediction split of src/tools/gtrain.cpp:293-333: edges are visited in a
+    seeded random order and removed while both endpoints still have degree > 1, until
+    frac of the undirected edges are removed; as many non-edges (distinct pairs u != v that
+    are not edges of the full graph) are sampled.  Returns (train_indptr, train_indices,
+    pos [2, m] int64, neg [2, m] int64)."""
+    V = len(indptr) - 1
+    deg = np.diff(indptr).astype(np.int64)
+    src = np.repeat(np.arange(V, dtype=np.int64), deg)
+    dst = indices.astype(np.int64)
+    keep = src < dst
+    src, dst = src[keep], dst[keep]
+    m = len(src)
+    want = int(m * frac)
+    order = np.argsort(_stream(seed, 11, m), kind="stable")
+    d = deg.copy()
+    removed = np.zeros(m, bool)
+    got = 0
+    so, do = src[order].tolist(), dst[order].tolist()
+    dl = d.tolist()
+    for i in range(m):
+        if got >= want:
+            break
+        a, b = so[i], do[i]
+        if dl[a] > 1 and dl[b] > 1:
+            dl[a] -= 1
+            dl[b] -= 1
+            removed[order[i]] = True
+            got += 1
+    tr_indptr, tr_indices = _csr_from_pairs_np(src[~removed], dst[~removed], V)
+    pos = np.stack([src[removed], dst[removed]])
+    full = np.sort(src * V + dst)
+    neg_keys = np.zeros(0, np.int64)
+    k = 0
+    while len(neg_keys) < got:
+        n = 2 * (got - len(neg_keys)) + 64
+        a = _below(_stream(seed, 100 + 2 * k, n), V).astype(np.int64)
+        b = _below(_stream(seed, 101 + 2 * k, n), V).astype(np.int64)
+        k += 1
+        lo, hi = np.minimum(a, b), np.maximum(a, b)
+        ok = lo != hi
+        kk = (lo * V + hi)[ok]
+        idx = np.searchsorted(full, kk).clip(max=len(full) - 1)
+        kk = kk[full[idx] != kk]
+        # keep first occurrences, in draw order, of pairs not drawn before
+        _, first = np.unique(kk, return_index=True)
+        kk = kk[np.sort(first)]
+        kk = kk[~np.isin(kk, neg_keys)]
+        neg_keys = np.concatenate([neg_keys, kk])[:got]
+    neg = np.stack([neg_keys // V, neg_keys % V])
+    return tr_indptr, tr_indices, pos, neg
+
+
 def vertex_counts(corpus, V):
     """Per-vertex occurrence counts of a corpus (the reference's vertex_cn, path.hpp:98)."""
     c = torch.as_tensor(corpus)

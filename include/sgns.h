@@ -185,8 +185,10 @@ sgns_status sgns_minibatch_update(int32_t d, int32_t n_batches, const int32_t* i
  * device array of about 1 MiB that every GPU loading the library holds until exit;
  * n is limited to 65536 minibatches (SGNS_EINVAL beyond).  The first call on a device
  * resolves that array's address and fills the sigmoid table, so make it before any
- * stream capture.  All calls share the array: calls that overlap on the GPU (other
- * streams, other threads) race on it.  Same arguments, results and limits otherwise. */
+ * stream capture.  Every call copies the kernel's status word back to the host and
+ * synchronises `stream` before it returns.  All calls share the array: calls that
+ * overlap on the GPU (other streams, other threads) race on it.  Same arguments,
+ * results and limits otherwise. */
 sgns_status sgns_minibatch_update_noalloc(int32_t d, int32_t n_batches, const int32_t* in_count,
                                           const int32_t* in_first, const int32_t* out_count,
                                           const int32_t* out_meta, const float* alpha,
@@ -202,6 +204,46 @@ sgns_status sgns_minibatch_update_noalloc(int32_t d, int32_t n_batches, const in
  * returns after the scores are written. */
 sgns_status sgns_link_scores(int32_t dtype, int32_t d, const void* table, int64_t V, const int32_t* pairs,
                              int64_t n, float* scores, void* stream);
+
+/* ---- corpus producer: information-oriented walks ------------------------------------
+ * Graphs are undirected CSR in device memory: indptr (V + 1 entries, indptr[0] = 0,
+ * indptr[V] = n_edges, non-decreasing) and indices (n_edges neighbour ids, each list
+ * strictly increasing; an edge appears in both endpoints' lists).  A malformed graph is
+ * SGNS_EINVAL, found by a device check before any kernel follows its pointers. */
+
+/* Common-neighbour count of every edge: cn[e] = |N(u) & N(v)| for edge e = (u, v) -- the
+ * edge data the information-oriented walker reads (candidate->data, include/walk.hpp:920),
+ * which the reference loads from a precomputed file (include/graph.hpp:826).  cn: device
+ * output of n_edges entries.  Ordered on stream; returns when the counts are written. */
+sgns_status sgns_edge_common_neighbors(const int64_t* indptr, const int32_t* indices, int64_t V, int64_t n_edges,
+                                       int32_t* cn, void* stream);
+
+typedef struct sgns_walk_options {
+  int64_t walker_num;  /* -w: walkers; walker k starts at vertex k % V (walk.hpp:503-506) */
+  int32_t min_length;  /* --min_L: moves made before the stop test applies (walk.hpp:404, 20) */
+  int32_t max_length;  /* vertices per walk at most, 1..1000 (the trainer reads at most 1000,
+                          dsgl.hpp:23; the reference walker has no cap) */
+  double r_threshold;  /* R of walk.hpp:24 (0.999): a walk stops once R*R < r_threshold or
+                          R < 0 (walk.hpp:868-874) */
+  uint64_t seed;       /* the walkers' random streams (counter-based; see below) */
+} sgns_walk_options;
+
+/* DistGER's information-oriented walks (InCoM, include/walk.hpp:818-1042: uniform neighbour
+ * candidates, the common-neighbour "trace" step that returns to the current vertex, and the
+ * stop rule on the correlation of path entropy and length, walk.hpp:260-387) over the
+ * graph, one walk per walker, written as corpus tokens: vertex ids with -1 after each walk
+ * in walker order (the layout of graph->local_corpus, path.hpp:96,110).  The reference
+ * draws from time-seeded generators; here walker k draws from its own SplitMix64 stream of
+ * `seed`, so a run is reproducible and equals the CPU restatement bit for bit.  The only
+ * rule that differs: a walk whose start vertex has only itself as neighbour ends after 64
+ * redraws (the reference redraws forever).  corpus: device output of cap entries;
+ * *n_tokens: the entries the walks yield, also set when cap is too small (then
+ * SGNS_EINVAL and nothing written; cap = 0 with corpus NULL just counts).  cn: the
+ * counts of sgns_edge_common_neighbors.  Uses library scratch memory (12 bytes per walker).
+ * Ordered on stream; returns after the corpus is written. */
+sgns_status sgns_info_walks(const sgns_walk_options* opt, const int64_t* indptr, const int32_t* indices,
+                            const int32_t* cn, int64_t V, int64_t n_edges, int32_t* corpus, int64_t cap,
+                            int64_t* n_tokens, void* stream);
 
 /* SGNS loss and its hand-written adjoint for n minibatches that index tables of V
  * rows (device pointers).  Minibatch b has inputs in_ids[in_ptr[b]..in_ptr[b+1]), the

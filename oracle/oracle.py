@@ -60,6 +60,15 @@ def lib():
         L.oracle_parse_walks.restype = i32
         L.oracle_link_scores.argtypes = [i32, i32, vp, i64, vp, i64, vp]
         L.oracle_link_scores.restype = i32
+        L.oracle_xlog2x_table.argtypes = [i32, vp]
+        L.oracle_xlog2x_table.restype = None
+        L.oracle_tanh_pos.argtypes = [ctypes.c_double]
+        L.oracle_tanh_pos.restype = ctypes.c_double
+        L.oracle_edge_common_neighbors.argtypes = [vp, vp, i64, vp]
+        L.oracle_edge_common_neighbors.restype = None
+        L.oracle_info_walks.argtypes = [vp, vp, vp, i64, i64, i32, i32, ctypes.c_double, ctypes.c_uint64, vp, i64,
+                                        ctypes.POINTER(i64), vp]
+        L.oracle_info_walks.restype = i32
         _lib = L
     return _lib
 
@@ -181,3 +190,43 @@ def minibatch(inputM, outputM, meta, first, alpha, acc64=False):
     lib().oracle_minibatch(1 if acc64 else 0, d, I, first, O, _p(meta), alpha, _p(inputM), _p(outputM),
                            _p(dIn), _p(dOut))
     return dIn, dOut
+
+
+def edge_common_neighbors(indptr, indices):
+    """cn[e] = |N(u) & N(v)| for every CSR edge e = (u, v) (walk_oracle.cpp)."""
+    indptr = np.ascontiguousarray(indptr, dtype=np.int64)
+    indices = np.ascontiguousarray(indices, dtype=np.int32)
+    cn = np.zeros(len(indices), np.int32)
+    lib().oracle_edge_common_neighbors(_p(indptr), _p(indices) if len(indices) else None, len(indptr) - 1,
+                                       _p(cn) if len(indices) else None)
+    return cn
+
+
+def info_walks(indptr, indices, cn, walker_num, min_length=20, max_length=80, r_threshold=0.999, seed=1):
+    """Information-oriented walks restated (walk_oracle.cpp).  Returns (corpus int32 with
+    -1 after each walk, lengths int32 per walker)."""
+    indptr = np.ascontiguousarray(indptr, dtype=np.int64)
+    indices = np.ascontiguousarray(indices, dtype=np.int32)
+    cn = np.ascontiguousarray(cn, dtype=np.int32)
+    V = len(indptr) - 1
+    n = ctypes.c_int64()
+    lengths = np.zeros(max(walker_num, 1), np.int32)
+    ie = _p(indices) if len(indices) else None
+    ce = _p(cn) if len(cn) else None
+    lib().oracle_info_walks(_p(indptr), ie, ce, V, walker_num, min_length, max_length, r_threshold, seed, None, 0,
+                            ctypes.byref(n), _p(lengths))
+    out = np.zeros(max(n.value, 1), np.int32)
+    rc = lib().oracle_info_walks(_p(indptr), ie, ce, V, walker_num, min_length, max_length, r_threshold, seed,
+                                 _p(out), len(out), ctypes.byref(n), None)
+    assert rc == 0
+    return out[:n.value], lengths[:walker_num]
+
+
+def xlog2x_table(n):
+    t = np.zeros(n, np.float64)
+    lib().oracle_xlog2x_table(n, _p(t))
+    return t
+
+
+def tanh_pos(x):
+    return lib().oracle_tanh_pos(float(x))

@@ -3,7 +3,7 @@
 // it produces the golden vectors that pin the oracle (tests/golden/make_golden.py) and
 // is never part of the product.
 //
-// Two stand-ins make a run deterministic without touching dsgl.hpp:
+// Three stand-ins make a run deterministic without touching dsgl.hpp:
 //   * omp_get_wtime (used only by the model-sync thread, dsgl.hpp:568-576) returns 0
 //     while compute threads run, so no sync round races with them; once every compute
 //     thread has returned it jumps ahead so the sync thread takes its exit branch
@@ -11,12 +11,23 @@
 //   * _mm_malloc/_mm_free are tracked so a compute thread's exit (it frees its first
 //     buffer, inputM, at dsgl.hpp:1409) is observable, and so the free of the
 //     never-initialised `stream` pointer (dsgl.hpp:1422) is ignored.
+//   * rand (used only by the sync thread, to pick one row per block of equal counts,
+//     dsgl.hpp:705) returns 0, so the pick is each block's first row.  The reference reads
+//     sync_ind[0] of a still empty vector when its pick in the first block is not row 0
+//     (dsgl.hpp:700-711), which crashes whenever the largest count is shared; the first row
+//     never triggers that read.  The round only runs after training, on one rank, where it
+//     copies rows out and back unchanged (allreduce of one rank, division by 1).
 //
 // usage: dsgl_ref <corpus.i32> <V> <out_prefix> [dsgl flags: -size -window ...]
 #include <omp.h>
 #include <xmmintrin.h>
 
+// every standard header dsgl.hpp and util.hpp include, before the rand stand-in below
+#include <algorithm>
 #include <atomic>
+#include <cmath>
+#include <cstring>
+#include <random>
 #include <cstdio>
 #include <cstdlib>
 #include <mutex>
@@ -62,12 +73,16 @@ void shim_mm_free(void* p) {
   free(p);
 }
 
+int shim_rand() { return 0; }
+
 #define omp_get_wtime shim_wtime
+#define rand shim_rand
 #define _mm_malloc shim_mm_malloc
 #define _mm_free shim_mm_free
 #include "dsgl.hpp"
 #undef _mm_free
 #undef _mm_malloc
+#undef rand
 #undef omp_get_wtime
 
 int main(int argc, char** argv) {
