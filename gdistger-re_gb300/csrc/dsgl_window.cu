@@ -115,8 +115,10 @@ __device__ __forceinline__ void store_row_from_smem(void* tab, int64_t row, int 
 }
 
 // kLoss: also accumulate the SGNS loss (compute_loss); without it no loss code is compiled
-// into the step.
-template <int S, int DCH, int OM, bool kLoss>
+// into the step.  DFIX: the hidden size as a compile-time constant (0: read from p.d).  With
+// d known, every shared-memory address of the step is a base register plus an immediate
+// offset and the column-range guards vanish; the arithmetic is the same either way.
+template <int S, int DCH, int OM, bool kLoss, int DFIX>
 __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
   extern __shared__ __align__(16) float smem[];
   float* exp_s = smem;
@@ -132,7 +134,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
   const int wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (wid >= p.workers) return;
 
-  const int d = p.d, w = p.window, K = p.K;
+  const int d = DFIX ? DFIX : p.d, w = p.window, K = p.K;
   const WinLayout L = win_layout(d, w, K, p.lmax);
   float* base = smem + kHdrWords + (threadIdx.x >> 5) * L.words;
   float* rows = base + L.rows;
@@ -482,28 +484,56 @@ size_t window_smem_bytes(int d, int window, int K, int lmax, int warps_per_cta) 
   return sizeof(float) * ((size_t)kHdrWords + (size_t)warps_per_cta * L.words);
 }
 
-template <int S, int DCH, int OM>
-static cudaError_t occupancy_t(int d, int w, int K, int lmax, int wpc, int* ctas) {
-  const size_t smem = window_smem_bytes(d, w, K, lmax, wpc);
-  cudaError_t e = cudaFuncSetAttribute(window_engine_kernel<S, DCH, OM, false>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas, window_engine_kernel<S, DCH, OM, false>, 32 * wpc, smem);
+// hidden sizes with their own kernel (training without the loss); others read d at run time
+constexpr int kFixedD[] = {64, 128, 256};
+inline int fixed_d(int d) {
+  for (int f : kFixedD)
+    if (d == f) return f;
+  return 0;
 }
 
-template <int S, int DCH, int OM, bool kLoss>
+template <int S, int DCH, int OM, bool kLoss, int DFIX>
+static cudaError_t occupancy_d(int d, int w, int K, int lmax, int wpc, int* ctas) {
+  const size_t smem = window_smem_bytes(d, w, K, lmax, wpc);
+  cudaError_t e = cudaFuncSetAttribute(window_engine_kernel<S, DCH, OM, kLoss, DFIX>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas, window_engine_kernel<S, DCH, OM, kLoss, DFIX>, 32 * wpc,
+                                                       smem);
+}
+template <int S, int DCH, int OM>
+static cudaError_t occupancy_t(int d, int w, int K, int lmax, int wpc, int* ctas) {
+  const int f = fixed_d(d);
+  if constexpr (DCH == 1) {
+    if (f == 64) return occupancy_d<S, DCH, OM, false, 64>(d, w, K, lmax, wpc, ctas);
+    if (f == 128) return occupancy_d<S, DCH, OM, false, 128>(d, w, K, lmax, wpc, ctas);
+  } else {
+    if (f == 256) return occupancy_d<S, DCH, OM, false, 256>(d, w, K, lmax, wpc, ctas);
+  }
+  return occupancy_d<S, DCH, OM, false, 0>(d, w, K, lmax, wpc, ctas);
+}
+
+template <int S, int DCH, int OM, bool kLoss, int DFIX>
 static cudaError_t launch_loss_t(const TrainParams& p, int wpc, cudaStream_t s) {
   const size_t smem = window_smem_bytes(p.d, p.window, p.K, p.lmax, wpc);
-  cudaError_t e = cudaFuncSetAttribute(window_engine_kernel<S, DCH, OM, kLoss>,
+  cudaError_t e = cudaFuncSetAttribute(window_engine_kernel<S, DCH, OM, kLoss, DFIX>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const int blocks = (p.workers + wpc - 1) / wpc;
-  window_engine_kernel<S, DCH, OM, kLoss><<<blocks, 32 * wpc, smem, s>>>(p);
+  window_engine_kernel<S, DCH, OM, kLoss, DFIX><<<blocks, 32 * wpc, smem, s>>>(p);
   return cudaGetLastError();
 }
 template <int S, int DCH, int OM>
 static cudaError_t launch_t(const TrainParams& p, int wpc, cudaStream_t s) {
-  return p.compute_loss ? launch_loss_t<S, DCH, OM, true>(p, wpc, s) : launch_loss_t<S, DCH, OM, false>(p, wpc, s);
+  if (p.compute_loss) return launch_loss_t<S, DCH, OM, true, 0>(p, wpc, s);
+  const int f = fixed_d(p.d);
+  if constexpr (DCH == 1) {
+    if (f == 64) return launch_loss_t<S, DCH, OM, false, 64>(p, wpc, s);
+    if (f == 128) return launch_loss_t<S, DCH, OM, false, 128>(p, wpc, s);
+  } else {
+    if (f == 256) return launch_loss_t<S, DCH, OM, false, 256>(p, wpc, s);
+  }
+  return launch_loss_t<S, DCH, OM, false, 0>(p, wpc, s);
 }
 
 // kernel variants: storage x column chunks per lane (d <= 128 or <= 256) x outputs per
