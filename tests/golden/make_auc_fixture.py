@@ -99,7 +99,8 @@ def reference_trainer(corpus, V, pos, neg, threads):
         pre = os.path.join(tmp, "out")
         flags = ["-size", str(TRAIN["size"]), "-window", str(TRAIN["window"]), "-negative", str(TRAIN["negative"]),
                  "-sample", str(TRAIN["sample"]), "-alpha", str(TRAIN["alpha"]), "-iter", str(TRAIN["iter"]),
-                 "-threads", str(threads + 1), "-min-count", "0", "-batch-size", "21", "-debug", "0"]
+                 "-threads", str(threads + 1), "-min-count", "0", "-batch-size", "21", "-debug", "0",
+                 "-eoutput", os.path.join(tmp, "emb.txt")]
         t0 = time.time()
         subprocess.run([REF_BIN, cpath, str(V), pre] + flags, check=True, stdout=subprocess.DEVNULL)
         wall = time.time() - t0
