@@ -37,14 +37,17 @@ for _p in (os.path.join(ROOT, "gdistger-re_gb300"), os.path.join(ROOT, "oracle")
 
 METRIC = "SGNS pairs/sec on 1 GB300 (BF16 batched vs plain FP32, same AUC) + HBM roofline %"
 
-# DRAM bytes (read + write) per pair of the persistent BF16 kernel, from one-pass ncu
-# captures (dram__bytes_read.sum + dram__bytes_write.sum) of a whole training launch of
-# each workload at 7 warps/CTA; profiles/window_engine_lj-cl_dram.md gives the command.
-# The small workload's tables fit in L2, so its figure does not scale to the large one.
-NCU_DRAM_BYTES_PER_PAIR = {"lj-cl": 1412.52e9 / 7597249326, "small": 48.00e9 / 675874507}
+# DRAM bytes (read + write) per pair of the persistent BF16 kernel, from a one-pass ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum) of one training launch of the
+# "lj-cl-1w" workload: the headline graph and tables with one walk per vertex instead of
+# ten (a tenth of the launch, a few GB on the device).  Traffic per pair is a steady-state
+# property of the same tables, so it scales to the headline launch by its pairs;
+# profiles/window_engine_lj-cl-1w_dram.md gives the command.  None until measured.
+NCU_DRAM_BYTES_PER_PAIR = {"lj-cl-1w": (82238461696 + 58338987264) / 759129518}
 
 WORKLOADS = {
     "lj-cl": dict(V=2238731, E=30_000_000, gamma=2.1, walks=10, mean=40, cap=80),
+    "lj-cl-1w": dict(V=2238731, E=30_000_000, gamma=2.1, walks=1, mean=40, cap=80),  # DRAM capture
     "small": dict(V=200_000, E=2_000_000, gamma=2.1, walks=10, mean=40, cap=80),
     "tiny": dict(V=5_000, E=50_000, gamma=2.1, walks=10, mean=40, cap=80),  # test-sized
 }
@@ -269,54 +272,110 @@ def _train_embedding(sgns, counts, corpus_np, V, engine, storage, device, pos=No
 
 
 def run_auc(args):
-    print(json.dumps(auc_suite(args.auc_vertices, cpu=not args.auc_skip_cpu, persistent_workers=args.auc_workers,
-                               plain_workers=args.auc_plain_workers)), flush=True)
+    sizes = [args.auc_vertices] if args.auc_vertices else None
+    print(json.dumps(auc_suite(sizes, persistent_workers=args.auc_workers, plain_workers=args.auc_plain_workers,
+                               plain_all_seeds=True)), flush=True)
 
 
-def auc_suite(V, cpu=True, persistent_workers=0, plain_workers=0):
-    """SBM graph with a 10% holdout, information-oriented walks (lengths 21-80, mean ~40);
-    the same corpus trained by every engine and (cpu=True) by the CPU reference restatement.
-    persistent_workers / plain_workers: worker counts (0 = each engine's default)."""
+AUC_FIXTURE = os.path.join(ROOT, "tests", "golden", "auc_sbm.json")
+
+
+def sbm_corpus_on_gpu(V, case, fx):
+    """The fixture's case rebuilt here: graph and holdout on the CPU from the recorded seeds
+    (synth's integer-only generators), common-neighbour counts and information-oriented
+    walks on the GPU (sgns_edge_common_neighbors, sgns_info_walks).  Returns (corpus on the
+    host, pos, neg, timing and identity of the corpus against the fixture's SHA-256)."""
+    import hashlib
     import torch
     import sgns
     import synth
-    import oracle
 
-    E = int(V * 2.73)
-    dev = "cuda"
-    ip, ix, _ = synth.sbm(V, E, blocks=4, ratio=20.0, seed=31, device=dev)
-    tr_ip, tr_ix, pos, neg = synth.holdout(ip, ix, 0.1, seed=32)
-    corpus = synth.information_walks(tr_ip, tr_ix, 10, 20, 80, 0.84, seed=33)
-    c = corpus.cpu().numpy().astype(np.int32)
-    counts = np.bincount(c[c >= 0], minlength=V).astype(np.int32)
-    ends = np.flatnonzero(c == -1)
-    lens = np.diff(np.concatenate([[-1], ends])) - 1
-    out = {"mode": "auc", "graph": "SBM V=%d E=%d 4 blocks p_in/p_out=20, 10%% holdout" % (V, ix.numel() // 2),
-           "walks": "10/vertex information-oriented, length mean %.1f (min %d, max %d)" % (lens.mean(), lens.min(), lens.max()),
-           "tokens": int(len(c)), "train": {**TRAIN, "iter": 1}}
-    for name, eng, sto in (("gpu_plain_fp32", "plain", "fp32"), ("gpu_persistent_fp32", "persistent", "fp32"),
-                           ("gpu_persistent_bf16", "persistent", "bf16")):
-        emb, st, auc = _train_embedding(sgns, counts, c, V, eng, sto, 0, pos, neg,
-                                        workers=plain_workers if eng == "plain" else persistent_workers)
-        out[name] = {"auc": auc, "pairs_per_s": st.pairs / st.train_ms * 1e3,
-                     "workers": st.workers, "roofline": _row_roofline(st)}
-    if cpu:
-        cores = host_cores()
-        wih, _, st = oracle.train(c, counts, d=TRAIN["size"], window=TRAIN["window"], negative=TRAIN["negative"],
-                                  iter=1, workers=cores, threads=cores, table_threads=TRAIN["threads"],
-                                  policy=oracle.POLICY_REF, storage=oracle.STORE_F32, table_size=TRAIN["table_size"],
-                                  sample=TRAIN["sample"], alpha=TRAIN["alpha"])
-        order, _, _, _ = oracle.vocab(counts)
-        emb = np.zeros((V, TRAIN["size"]), np.float32)
-        emb[order] = wih
-        out["cpu_reference_fp32"] = {"auc": synth.link_auc(emb, pos, neg),
-                                     "pairs_per_s": st["pairs"] / st["train_seconds"], "threads": cores,
-                                     "kind": "oracle restatement of include/dsgl.hpp, reference buffer policy"}
-    b = out["gpu_persistent_bf16"]["auc"]
-    out["bf16_minus_fp32_auc"] = b - out["gpu_persistent_fp32"]["auc"]
-    if "cpu_reference_fp32" in out:
-        out["gpu_plain_fp32_minus_cpu_auc"] = out["gpu_plain_fp32"]["auc"] - out["cpu_reference_fp32"]["auc"]
-        out["gpu_persistent_bf16_minus_cpu_auc"] = b - out["cpu_reference_fp32"]["auc"]
+    g, wk, sd = fx["graph"], fx["walks"], case["seeds"]
+    ip, ix, _ = synth.sbm_csr(V, int(g["edges_per_vertex"] * V), g["blocks"], g["ratio"], seed=sd["graph"])
+    tip, tix, pos, neg = synth.holdout_csr(ip, ix, g["holdout"], seed=sd["holdout"])
+    dip, dix = torch.from_numpy(tip).cuda(), torch.from_numpy(tix).cuda()
+    dcn = torch.empty(len(tix), dtype=torch.int32, device="cuda")
+    n = wk["walks_per_vertex"] * V
+    sgns.edge_common_neighbors(dip, dix, dcn)  # warm-up of both entry points on this graph
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sgns.edge_common_neighbors(dip, dix, dcn)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    corpus, n_tok = sgns.info_walks(dip, dix, dcn, n, wk["min_length"], wk["max_length"], wk["r_threshold"],
+                                    sd["walks"], trace=wk["trace_steps"])
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    c = corpus.cpu().numpy()
+    moves = n_tok - 2 * n  # appended vertices after each walk's start (tokens minus starts and -1s)
+    info = {"tokens": int(n_tok), "corpus_identical": hashlib.sha256(c.tobytes()).hexdigest() == case["corpus_sha256"],
+            "common_neighbors_ms": 1e3 * (t1 - t0), "walks_ms": 1e3 * (t2 - t1),
+            "walk_tokens_per_s": n_tok / (t2 - t1), "walkers": n, "edges": int(len(tix) // 2),
+            # the walker's gathers per move: two indptr pairs, one neighbour id, one count (40 B),
+            # made once per pass over the walks (two passes: lengths, then tokens)
+            "walk_gather_GBs": 2 * 40.0 * moves / (t2 - t1) / 1e9}
+    del dip, dix, dcn, corpus
+    return c, pos, neg, info
+
+
+def auc_suite(sizes=None, persistent_workers=0, plain_workers=0, plain_all_seeds=False):
+    """Link-prediction AUC of every GPU engine on exactly the corpora of the committed CPU
+    fixture (tests/golden/auc_sbm.json: the survey's configuration 2 -- 4-block SBM, 10%
+    holdout, 10 information-oriented walks per vertex -- at 100k and 1.1M vertices, one
+    graph/holdout/walk seed triple per case), against the CPU trainer's AUC recorded there.
+    The plain fp32 engine (one launch per step) runs on every seed at the smallest size and
+    on the first seed at larger sizes unless plain_all_seeds."""
+    import torch
+    import sgns
+    import synth
+
+    fx = json.load(open(AUC_FIXTURE))
+    by_v = {}
+    for c in fx["cases"]:
+        by_v.setdefault(c["V"], []).append(c)
+    sizes = sorted(by_v) if not sizes else sizes
+    out = {"mode": "auc on the CPU fixture's corpora", "fixture": os.path.relpath(AUC_FIXTURE, ROOT),
+           "graph": fx["graph"], "walks": fx["walks"], "train": {**TRAIN, "iter": 1}}
+    arms = (("gpu_plain_fp32", "plain", "fp32"), ("gpu_persistent_fp32", "persistent", "fp32"),
+            ("gpu_persistent_bf16", "persistent", "bf16"))
+    for V in sizes:
+        cases = sorted(by_v[V], key=lambda c: c["seed"])
+        res = {a[0]: {"per_seed": {}, "pairs_per_s": [], "workers": None} for a in arms}
+        walks = []
+        for k, case in enumerate(cases):
+            c, pos, neg, info = sbm_corpus_on_gpu(V, case, fx)
+            walks.append(info)
+            counts = np.bincount(c[c >= 0], minlength=V).astype(np.int32)
+            for name, eng, sto in arms:
+                if eng == "plain" and k > 0 and V != min(sizes) and not plain_all_seeds:
+                    continue
+                w = plain_workers if eng == "plain" else persistent_workers
+                _, st, auc = _train_embedding(sgns, counts, c, V, eng, sto, 0, pos, neg, workers=w)
+                res[name]["per_seed"][str(case["seed"])] = auc
+                res[name]["pairs_per_s"].append(st.pairs / st.train_ms * 1e3)
+                res[name]["workers"] = st.workers
+            torch.cuda.empty_cache()
+        cpu = {str(c["seed"]): c["cpu_trainer"]["auc"] for c in cases if "cpu_trainer" in c}
+        cpu_mean = float(np.mean(list(cpu.values()))) if cpu else None
+        entry = {"seeds": [c["seed"] for c in cases], "corpora_identical": all(w["corpus_identical"] for w in walks),
+                 "tokens": [w["tokens"] for w in walks],
+                 "cpu_trainer": {"per_seed": cpu, "mean": cpu_mean,
+                                 "std": float(np.std(list(cpu.values()))) if cpu else None,
+                                 "threads": cases[0].get("cpu_trainer", {}).get("threads")},
+                 "reference": {str(c["seed"]): c["reference"]["auc"] for c in cases if "reference" in c}}
+        for name, _, _ in arms:
+            v = list(res[name]["per_seed"].values())
+            r = res[name]
+            r["mean"] = float(np.mean(v)) if v else None
+            r["std"] = float(np.std(v)) if v else None
+            r["pairs_per_s"] = float(np.mean(r["pairs_per_s"])) if r["pairs_per_s"] else None
+            # same seeds only: the difference to the CPU trainer on the identical corpora
+            common = [s for s in r["per_seed"] if s in cpu]
+            r["minus_cpu_trainer"] = (float(np.mean([r["per_seed"][s] - cpu[s] for s in common]))
+                                      if common else None)
+            entry[name] = r
+        entry["walks"] = walks
+        out[str(V)] = entry
     return out
 
 
@@ -367,20 +426,72 @@ def reference_minibatches(corpus, V, n, w, K, seed, device):
     return in_ids, in_ptr, first, out_ids, out_ptr, meta
 
 
-def run_minibatch_error(args):
-    """bf16 form, per minibatch: the fp32 update (the trainers' arithmetic) and the
-    stochastically rounded bf16 rows it stores, against an fp64 oracle, on 1000
-    reference-shaped minibatches over the rows of a bf16 training run."""
+def minibatch_error(tr, corpus, V, n=1000, seed=7):
+    """Configuration 3's error statement on a trained BF16 table: n reference-shaped
+    minibatches (a target and its window from each of two walks of the corpus, K shared
+    negatives) over the table's rows, stepped on the GPU by sgns_minibatch_update_bf16 --
+    the step arithmetic followed by the BF16 trainers' stochastically rounded write-back --
+    and by an fp64 oracle step from the same (bf16-valued) rows.  Per minibatch: the largest
+    relative row error ||r_bf16 - r_fp64|| / ||r_fp64|| over its rows; also the fp32 update
+    (sgns_minibatch_update) against the fp64 update, and the mean signed rounding error in
+    bf16 units in the last place (stochastic rounding is unbiased: near 0)."""
     import torch
     import sgns
-    import synth
     import oracle
 
-    wl = WORKLOADS["small"]
     dev = "cuda"
-    ip, ix = synth.chung_lu(wl["V"], wl["E"], wl["gamma"], seed=2024, device=dev)
-    L = synth.walk_lengths(wl["V"] * 2, "geometric", mean=40, cap=80, seed=5, device=dev)
-    corpus = synth.random_walks(ip, ix, 2, L, seed=6)
+    wih, woh = tr.embeddings(0), tr.embeddings(1)  # bf16 values, sorted-row order
+    row_of = np.empty(V, np.int64)
+    row_of[tr.order()] = np.arange(V)
+    ii, ip_, ff, oo, op_, mm = reference_minibatches(corpus, V, n, TRAIN["window"], TRAIN["negative"], seed, dev)
+    xin = wih[row_of[np.asarray(ii)]]
+    xout = woh[row_of[np.asarray(oo)]]
+    del wih, woh
+    tt = lambda a, dt=torch.int32: torch.tensor(np.asarray(a), dtype=dt, device=dev)
+    in_count, out_count, first, meta = tt(np.diff(ip_)), tt(np.diff(op_)), tt(ff), tt(mm)
+    alpha = torch.full((n,), TRAIN["alpha"], dtype=torch.float32, device=dev)
+    dxin, dxout = torch.tensor(xin, device=dev), torch.tensor(xout, device=dev)
+    d_in, d_out = torch.empty_like(dxin), torch.empty_like(dxout)
+    sgns.minibatch_update(TRAIN["size"], in_count, first, out_count, meta, alpha, dxin, dxout, d_in, d_out)
+    b_in = torch.empty(dxin.shape, dtype=torch.int16, device=dev)
+    b_out = torch.empty(dxout.shape, dtype=torch.int16, device=dev)
+    sgns.minibatch_update_bf16(TRAIN["size"], in_count, first, out_count, meta, alpha, dxin, dxout, b_in, b_out,
+                               seed=0x5EED)
+    widen = lambda b: (b.cpu().numpy().view(np.uint16).astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+    gi, go = d_in.cpu().numpy().astype(np.float64), d_out.cpu().numpy().astype(np.float64)
+    ri, ro = widen(b_in), widen(b_out)
+    upd_err, row_err, ulp_err = [], [], []
+    oi = oo_ = 0
+    for b in range(n):
+        I, O = ip_[b + 1] - ip_[b], op_[b + 1] - op_[b]
+        x0, o0 = xin[oi:oi + I].astype(np.float64), xout[oo_:oo_ + O].astype(np.float64)
+        dIn, dOut = oracle.minibatch(x0, o0, mm[op_[b]:op_[b + 1]], ff[b], TRAIN["alpha"], acc64=True)
+        for got, ref, base, stored in ((gi[oi:oi + I], dIn, x0, ri[oi:oi + I]), (go[oo_:oo_ + O], dOut, o0, ro[oo_:oo_ + O])):
+            nref = np.linalg.norm(ref)
+            if nref > 0:
+                upd_err.append(np.linalg.norm(got - ref) / nref)
+            new64 = base + ref
+            row_err.append(np.max(np.linalg.norm(stored - new64, axis=1) / np.maximum(np.linalg.norm(new64, axis=1), 1e-30)))
+            nz = new64 != 0
+            ulp = 2.0 ** (np.floor(np.log2(np.abs(new64[nz]))) - 7)
+            ulp_err.append(float(np.mean((stored[nz] - new64[nz]) / ulp)))
+        oi += I
+        oo_ += O
+    q = lambda a: {"median": float(np.median(a)), "p99": float(np.quantile(a, 0.99)), "max": float(np.max(a))}
+    return {"minibatches": n, "d": TRAIN["size"], "rows": int(len(ii) + len(oo)),
+            "bf16_stored_row_rel_err_vs_fp64": q(row_err), "fp32_update_rel_err_vs_fp64": q(upd_err),
+            "bf16_mean_signed_err_ulp": float(np.mean(ulp_err)),
+            "source": "rows of the trained BF16 table, stepped by sgns_minibatch_update_bf16 (the trainers' "
+                      "arithmetic and stochastically rounded write-back); fp64 oracle step from the same rows"}
+
+
+def run_minibatch_error(args):
+    """--mb-error: minibatch_error on a one-pass BF16 training of the workload's corpus."""
+    import torch
+    import sgns
+
+    wl = WORKLOADS[args.workload]
+    corpus, _, _, _, _ = make_corpus(wl, 0, torch.device("cuda", 0))
     c = corpus.cpu().numpy().astype(np.int32)
     counts = np.bincount(c[c >= 0], minlength=wl["V"]).astype(np.int32)
     opt = sgns.default_options(iter=1, storage="bf16", engine="persistent", device=0, debug=0, **TRAIN)
@@ -388,47 +499,8 @@ def run_minibatch_error(args):
         t.set_vocab(counts)
         t.upload(c)
         t.train()
-        wih, woh = t.embeddings(0), t.embeddings(1)  # bf16 values, sorted-row order
-        row_of = np.empty(wl["V"], np.int64)
-        row_of[t.order()] = np.arange(wl["V"])
-    ii, ip_, ff, oo, op_, mm = reference_minibatches(corpus, wl["V"], 1000, TRAIN["window"], TRAIN["negative"], 7, dev)
-    xin = wih[row_of[np.asarray(ii)]]
-    xout = woh[row_of[np.asarray(oo)]]
-    tt = lambda a, dt=torch.int32: torch.tensor(np.asarray(a), dtype=dt, device=dev)
-    in_count = tt(np.diff(ip_))
-    out_count = tt(np.diff(op_))
-    alpha = torch.full((1000,), TRAIN["alpha"], dtype=torch.float32, device=dev)
-    d_in = torch.empty((len(ii), TRAIN["size"]), device=dev)
-    d_out = torch.empty((len(oo), TRAIN["size"]), device=dev)
-    sgns.minibatch_update(TRAIN["size"], in_count, tt(ff), out_count, tt(mm), alpha, torch.tensor(xin, device=dev),
-                          torch.tensor(xout, device=dev), d_in, d_out)
-    gi, go = d_in.cpu().numpy().astype(np.float64), d_out.cpu().numpy().astype(np.float64)
-    rng = np.random.default_rng(9)
-
-    def sr_bf16(x):  # the rounding rule of the kernels: add 16 uniform bits, truncate
-        u = x.astype(np.float32).view(np.uint32).astype(np.uint64)
-        r = rng.integers(0, 1 << 16, size=u.shape, dtype=np.uint64)
-        return (((u + r) >> 16).astype(np.uint32) << 16).view(np.float32).astype(np.float64)
-
-    upd_err, row_err = [], []
-    oi = oo_ = 0
-    for b in range(1000):
-        I, O = ip_[b + 1] - ip_[b], op_[b + 1] - op_[b]
-        x0, o0 = xin[oi:oi + I].astype(np.float64), xout[oo_:oo_ + O].astype(np.float64)
-        dIn, dOut = oracle.minibatch(x0, o0, mm[op_[b]:op_[b + 1]], ff[b], TRAIN["alpha"], acc64=True)
-        for got, ref, base in ((gi[oi:oi + I], dIn, x0), (go[oo_:oo_ + O], dOut, o0)):
-            nref = np.linalg.norm(ref)
-            if nref > 0:
-                upd_err.append(np.linalg.norm(got - ref) / nref)
-            new64 = base + ref
-            new_bf16 = sr_bf16(base + got)
-            row_err.append(np.max(np.linalg.norm(new_bf16 - new64, axis=1) / np.maximum(np.linalg.norm(new64, axis=1), 1e-30)))
-        oi += I
-        oo_ += O
-    q = lambda a: {"median": float(np.median(a)), "p99": float(np.quantile(a, 0.99)), "max": float(np.max(a))}
-    print(json.dumps({"mode": "minibatch-error", "minibatches": 1000, "d": TRAIN["size"],
-                      "fp32_update_rel_err_vs_fp64": q(upd_err), "bf16_stored_row_rel_err_vs_fp64": q(row_err)}),
-          flush=True)
+        res = minibatch_error(t, corpus, wl["V"])
+    print(json.dumps({"mode": "minibatch-error", "workload": args.workload, **res}), flush=True)
 
 
 def run_sweep(args):
@@ -677,8 +749,7 @@ def main():
     ap.add_argument("--skip-extras", action="store_true", help="only the timed bf16 steps (profiling runs)")
     ap.add_argument("--wpc", type=int, default=0, help="warps per CTA of the persistent engine (0 = autotune)")
     ap.add_argument("--auc", action="store_true", help="link-prediction AUC of every engine and the CPU reference")
-    ap.add_argument("--auc-vertices", type=int, default=100000)
-    ap.add_argument("--auc-skip-cpu", action="store_true")
+    ap.add_argument("--auc-vertices", type=int, default=0, help="one fixture size (0 = every size)")
     ap.add_argument("--auc-workers", type=int, default=0, help="persistent-engine workers in --auc (0 = default)")
     ap.add_argument("--auc-plain-workers", type=int, default=0, help="plain-engine workers in --auc (0 = default)")
     ap.add_argument("--mb-error", action="store_true", help="bf16 per-minibatch error against fp64")
@@ -760,10 +831,12 @@ def main():
     achieved = bytes_per_launch / launch_s / 1e9
     peak = pk["hbm_gbs"] if pk else 6800.0
     table_traffic = (st_last.row_loads + st_last.row_stores + 2 * st_last.output_rows) * TRAIN["size"] * 2
+    # DRAM bytes per pair of the lj-cl tables (captured on the lj-cl-1w workload) x pairs
+    bpp = NCU_DRAM_BYTES_PER_PAIR.get("lj-cl-1w") if args.workload in ("lj-cl", "lj-cl-1w") else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": (NCU_DRAM_BYTES_PER_PAIR[args.workload] * pairs / args.steps
-                            if args.workload in NCU_DRAM_BYTES_PER_PAIR else None),
-                "traffic_source": "ncu DRAM bytes per pair of this workload x pairs per launch",
+                "traffic": bpp * pairs / args.steps if bpp else None,
+                "traffic_source": "ncu DRAM read + write bytes per pair of one lj-cl-1w launch (same graph and "
+                                  "tables, 1 walk per vertex) x pairs per launch",
                 "peak_source": "measured" if pk else "fallback",
                 "algorithmic_bytes_per_launch": bytes_per_launch,
                 "table_bytes_per_launch": float(table_traffic + 4 * n_tok),
@@ -772,27 +845,38 @@ def main():
             "warmup": args.warmup, "ms_per_step": 1e3 * elapsed_max / args.steps,
             "timing": "CUDA events on the launching stream around each step; wall clock beside",
             "wall_ms_per_step": 1e3 * wall_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16 tables (stochastic rounding on write-back), fp32 arithmetic",
             "data": "synthetic (seeded Chung-Lu stand-in for LiveJournal; random walks)",
-            "config": {"workload": "%s: Chung-Lu V=%d E=%d gamma=%.1f, 10 walks/vertex geometric(mean %d, cap %d) "
+            "config": {"workload": "%s: Chung-Lu V=%d E=%d gamma=%.1f, %d walks/vertex geometric(mean %d, cap %d) "
                                    "on the 90%% training graph, %d tokens per rank" %
-                                   (args.workload, wl["V"], edges, wl["gamma"], wl["mean"], wl["cap"], n_tok),
+                                   (args.workload, wl["V"], edges, wl["gamma"], wl["walks"], wl["mean"], wl["cap"],
+                                    n_tok),
                        "engine": "persistent", "storage": "bf16-sr", "workers": st_last.workers,
                        "warps_per_cta": st_last.warps_per_cta, "l2": "inputs larger than L2 (no flush)",
                        "parallelism": "replicas x%d" % ws, **TRAIN},
             "roofline": roofline, "gpu_launches": args.steps, "clocks": clk,
             "steps_per_launch": st_last.steps, "pairs_per_launch": st_last.pairs, "corpus_gen_s": gen_s}
 
+    if not args.skip_extras and rank == 0:
+        try:  # configuration 3's per-minibatch error, on the headline's trained bf16 tables
+            line["minibatch_error"] = minibatch_error(tr, corpus, wl["V"])
+        except Exception as e:
+            line["minibatch_error"] = {"error": "%s: %s" % (type(e).__name__, e)}
     if not args.skip_extras:
         # e2e through the reference-facing call, host buffers in, statistics out
         # one untimed call first: the first GPU read of a pinned buffer sets up its host-page
         # translations (about 0.2 s for 3.2 GB); a caller that reuses the buffer pays it once
+        # the trained input table comes back too, as the reference's my_saveModel reads it
+        emb_host = torch.empty((wl["V"], TRAIN["size"]), dtype=torch.float32, pin_memory=True)
         tr.train_corpus_ptr(corpus_host.data_ptr(), n_tok)
+        tr.embeddings_to(0, emb_host.data_ptr())
         e2e_t, e2e_pairs, e2e_kernel_ms = [], 0, []
         for it in range(max(1, args.steps)):
             torch.cuda.synchronize()
             t1 = time.perf_counter()
             s2 = tr.train_corpus_ptr(corpus_host.data_ptr(), n_tok)
+            tr.embeddings_to(0, emb_host.data_ptr())
             t2 = time.perf_counter()
             e2e_t.append(t2 - t1)
             e2e_pairs += s2.pairs
@@ -800,11 +884,38 @@ def main():
         e2e_max = max_over_ranks(sum(e2e_t), dist, dev)
         e2e_pairs_all = sum_over_ranks(float(e2e_pairs), dist, dev)
         line["e2e"] = {"value": e2e_pairs_all / e2e_max, "unit": "pairs/s", "h2d_bytes_per_step": 4 * n_tok,
-                       "d2h_bytes_per_step": 80,
+                       "d2h_bytes_per_step": 96 + 4 * wl["V"] * TRAIN["size"],
+                       "read_back": "statistics and the trained Wih (fp32, V x d) through sgns_get_embeddings",
                        "outside_kernel_ms_per_step": 1e3 * float(np.mean(e2e_t)) - float(np.mean(e2e_kernel_ms))}
         line["e2e"]["warmup"] = 1
-        line["gpu_launches"] = args.steps + 3 * max(1, args.steps)
+        # per e2e step: id->row mapping, longest-walk scan, training launch, the chunked
+        # bf16 -> fp32 widening of Wih (V*d / 8M elements per launch)
+        widen = -(-wl["V"] * TRAIN["size"] // (8 << 20))
+        line["gpu_launches"] = args.steps + (3 + widen) * max(1, args.steps)
         tr.close()
+        del emb_host
+        # the same engine with fp32 tables on the same corpus: what bf16 storage buys
+        try:
+            fopt = sgns.default_options(iter=1, storage="fp32", engine="persistent", device=local, debug=0,
+                                        warps_per_cta=args.wpc, **TRAIN)
+            with sgns.Trainer(fopt) as ft:
+                ft.set_vocab(counts)
+                ft.upload(host_np)
+                ft.train()
+                fms, fpairs, frb = [], 0, 0
+                for _ in range(max(1, args.steps)):
+                    fs = ft.train()
+                    fms.append(fs.train_ms)
+                    fpairs += fs.pairs
+                    frb += fs.row_bytes
+            fval = fpairs / (float(np.sum(fms)) / 1e3)
+            fach = frb / len(fms) / (float(np.mean(fms)) / 1e3) / 1e9
+            line["fp32_persistent"] = {"value": fval, "unit": "pairs/s", "kernel_ms": float(np.mean(fms)),
+                                       "workers": fs.workers, "warps_per_cta": fs.warps_per_cta,
+                                       "roofline_frac": fach / peak, "row_GBs": fach}
+            line["bf16_over_fp32_persistent"] = value / ws / fval
+        except Exception as e:
+            line["fp32_persistent"] = {"error": "%s: %s" % (type(e).__name__, e)}
         # The remaining extras use no collective; one that fails is recorded in the line
         # (the timed numbers above stand) instead of losing the line.
         def failed(e):
@@ -832,7 +943,13 @@ def main():
             # Link-prediction quality: the Chung-Lu graph has no community structure to
             # predict, so the engines are compared on a labelled SBM (same training settings).
             try:
-                line["auc_sbm"] = auc_suite(100_000, cpu=False)
+                t0 = time.time()
+                line["auc_sbm"] = auc_suite()
+                line["auc_sbm"]["seconds"] = time.time() - t0
+                sizes = [int(k) for k in line["auc_sbm"] if k.isdigit()]
+                if sizes and line["auc_sbm"][str(max(sizes))].get("walks"):  # the corpus producer, config 2 size
+                    line["walks"] = {**line["auc_sbm"][str(max(sizes))]["walks"][0],
+                                     "graph": "SBM V=%d, 4 blocks, 10 information-oriented walks per vertex" % max(sizes)}
             except Exception as e:
                 line["auc_sbm"] = failed(e)
             try:

@@ -57,14 +57,17 @@ __global__ void map_corpus_kernel(const int32_t* ids, const int32_t* row_of, int
 }
 
 // ---- explicit-row minibatch update (the step arithmetic of both trainers) ----------
-template <int DCH>
+// kRound: instead of the updates, write each updated row (row + update) as bf16 bits with
+// the trainers' stochastic rounding (RowIO<STORE_BF16>::store4), event keys from sr_seed
+// and the minibatch index; d_in / d_out then point to uint16 rows.
+template <int DCH, bool kRound = false>
 __global__ void __launch_bounds__(32) minibatch_kernel(int d, int imax, int omax, const int32_t* in_count,
                                                        const int32_t* in_first, const int32_t* out_count,
                                                        const int32_t* out_meta_all, const float* alpha,
                                                        const int64_t* in_off, const int64_t* out_off,
                                                        const float* in_rows, const float* out_rows,
                                                        float* d_in, float* d_out, const float* exp_table,
-                                                       int32_t* status) {
+                                                       int32_t* status, uint64_t sr_seed = 0) {
   extern __shared__ __align__(16) float smem[];
   const int b = blockIdx.x, lane = lane_id();
   const int I = in_count[b], first = in_first[b], O = out_count[b];
@@ -103,17 +106,41 @@ __global__ void __launch_bounds__(32) minibatch_kernel(int d, int imax, int omax
   float loss = 0.f;
   forward_gradient<kOMax>(I, first, O, d, in_ptr, outI, meta, exp_s, alpha[b], corrP, false, loss);
   float4 md[kOMax][DCH];
-  float* gdin = d_in + in_off[b] * d;
-  backward<kOMax, DCH>(I, O, d, in_ptr, [&](int pp, int q, float4& r0, float4& r1) { out_chunk_pair(outI, d, pp, q, r0, r1); }, corrP, md,
-                       [&](int j, int q, float4 a) { reinterpret_cast<float4*>(gdin + (size_t)j * d)[q] = a; });
-  float* gdout = d_out + out_off[b] * d;
+  if (!kRound) {
+    float* gdin = d_in + in_off[b] * d;
+    backward<kOMax, DCH>(I, O, d, in_ptr, [&](int pp, int q, float4& r0, float4& r1) { out_chunk_pair(outI, d, pp, q, r0, r1); }, corrP, md,
+                         [&](int j, int q, float4 a) { reinterpret_cast<float4*>(gdin + (size_t)j * d)[q] = a; });
+    float* gdout = d_out + out_off[b] * d;
 #pragma unroll
-  for (int i = 0; i < kOMax; i++)
+    for (int i = 0; i < kOMax; i++)
 #pragma unroll
-    for (int t = 0; t < DCH; t++) {
-      const int q = lane + 32 * t;
-      if (i < O && q < d4) reinterpret_cast<float4*>(gdout + (size_t)i * d)[q] = md[i][t];
-    }
+      for (int t = 0; t < DCH; t++) {
+        const int q = lane + 32 * t;
+        if (i < O && q < d4) reinterpret_cast<float4*>(gdout + (size_t)i * d)[q] = md[i][t];
+      }
+  } else {
+    // rows j of the inputs: event key EV_WALK0 of minibatch b; row index = j (outputs: the
+    // key EV_NEG, row index = i) -- the same rounding rule and hash as the trainers' stores
+    const uint64_t ev_in = sr_event_key(sr_seed, EV_WALK0, 0u, (uint64_t)b);
+    const uint64_t ev_out = sr_event_key(sr_seed, EV_NEG, 0u, (uint64_t)b);
+    uint16_t* gin16 = reinterpret_cast<uint16_t*>(d_in) + in_off[b] * d;
+    backward<kOMax, DCH>(I, O, d, in_ptr, [&](int pp, int q, float4& r0, float4& r1) { out_chunk_pair(outI, d, pp, q, r0, r1); }, corrP, md,
+                         [&](int j, int q, float4 a) {
+                           const float4 x = reinterpret_cast<const float4*>(gin + (size_t)j * d)[q];
+                           RowIO<STORE_BF16>::store4(gin16, j, d, q, add4(x, a), ev_in);
+                         });
+    uint16_t* gout16 = reinterpret_cast<uint16_t*>(d_out) + out_off[b] * d;
+#pragma unroll
+    for (int i = 0; i < kOMax; i++)
+#pragma unroll
+      for (int t = 0; t < DCH; t++) {
+        const int q = lane + 32 * t;
+        if (i < O && q < d4) {
+          const float4 o = reinterpret_cast<const float4*>(gout + (size_t)i * d)[q];
+          RowIO<STORE_BF16>::store4(gout16, i, d, q, add4(o, md[i][t]), ev_out);
+        }
+      }
+  }
 }
 
 // each walk start scans forward to its separator (at most kMaxSentence tokens); one
@@ -151,6 +178,24 @@ __global__ void prefix_offsets_kernel(const int32_t* cnt_a, const int32_t* cnt_b
 
 }  // namespace
 
+// bf16 bits -> fp32 (exact), 4 elements per thread; n % 4 == 0 (d is a multiple of 4)
+__global__ void widen_bf16_kernel(const uint2* __restrict__ src, float4* __restrict__ dst, int64_t n4) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint2 u = src[i];
+    dst[i] = make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xFFFF0000u), __uint_as_float(u.y << 16),
+                         __uint_as_float(u.y & 0xFFFF0000u));
+  }
+}
+
+cudaError_t launch_widen_bf16(const void* src, float* dst, int64_t n, cudaStream_t s) {
+  const int64_t n4 = n / 4;
+  if (n4 == 0) return cudaSuccess;
+  const int64_t blocks = (n4 + 255) / 256;
+  widen_bf16_kernel<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, s>>>(static_cast<const uint2*>(src),
+                                                                             reinterpret_cast<float4*>(dst), n4);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_init_wih(void* wih, int storage, int64_t V, int32_t d, const LcgJumps* jumps,
                             cudaStream_t s) {
   const int64_t n = V * d;
@@ -174,6 +219,37 @@ cudaError_t launch_max_walk(const int32_t* rows, int64_t n, int32_t* out, cudaSt
   int64_t blocks = (n + 255) / 256;
   if (blocks > 152 * 32) blocks = 152 * 32;
   max_walk_kernel<<<(unsigned)blocks, 256, 0, s>>>(rows, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_minibatch_bf16(int d, int n, int imax, const int32_t* in_count, const int32_t* in_first,
+                                  const int32_t* out_count, const int32_t* out_meta, const float* alpha,
+                                  const float* in_rows, const float* out_rows, uint16_t* new_in, uint16_t* new_out,
+                                  uint64_t sr_seed, const float* exp_table, int64_t* offsets, int32_t* status,
+                                  cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  int64_t* in_off = offsets;
+  int64_t* out_off = offsets + n;
+  prefix_offsets_kernel<<<1, 1, 0, s>>>(in_count, out_count, n, in_off, out_off);
+  const int DP = d + 4;
+  const size_t smem = sizeof(float) * (1004 + (size_t)imax * DP + (size_t)kOMax * d +
+                                       (size_t)imax * (kOMax + 2) * 2 + kOMax + 4);
+  float* a = reinterpret_cast<float*>(new_in);
+  float* b = reinterpret_cast<float*>(new_out);
+  cudaError_t e;
+  if (d > 128) {
+    e = cudaFuncSetAttribute(minibatch_kernel<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    minibatch_kernel<2, true><<<n, 32, smem, s>>>(d, imax, kOMax, in_count, in_first, out_count, out_meta, alpha,
+                                                  in_off, out_off, in_rows, out_rows, a, b, exp_table, status,
+                                                  sr_seed);
+  } else {
+    e = cudaFuncSetAttribute(minibatch_kernel<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    minibatch_kernel<1, true><<<n, 32, smem, s>>>(d, imax, kOMax, in_count, in_first, out_count, out_meta, alpha,
+                                                  in_off, out_off, in_rows, out_rows, a, b, exp_table, status,
+                                                  sr_seed);
+  }
   return cudaGetLastError();
 }
 

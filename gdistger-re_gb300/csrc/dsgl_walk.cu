@@ -15,7 +15,8 @@
 // with adj[c][0] == c ends it; before the first move u == c draws again (at most 64 times
 // in a row, then the walk ends -- the reference spins forever there); p = uniform;
 // pa = ((1 / (ds - cn)) max(ds, du)) / min(ds, du); trace = tanh(pa) <= p; u is appended,
-// then c again on a trace; the walk moves to u only without one.  Every appended vertex
+// then c again on a trace; the walk moves to u only without one.  With trace steps off
+// there is no p draw and every move goes on to u.  Every appended vertex
 // updates the correlation state (Correlation::iterate, step 1) with f = its earlier visits,
 // and the walk stops after more than min_length moves once R*R < r_threshold or R < 0
 // (walk.hpp:868-874), or when it holds max_length vertices.
@@ -96,6 +97,7 @@ struct WalkArgs {
   int32_t min_length, max_length;
   double r_threshold;
   uint64_t seed;
+  int32_t trace;           // 1: the trace step of walk.hpp:920-1031; 0: moves only
   int32_t* lengths;        // pass 1 output
   const int64_t* offsets;  // pass 2 input (exclusive scan of length + 1)
   int32_t* corpus;         // pass 2 output
@@ -140,13 +142,17 @@ __global__ void __launch_bounds__(256) info_walk_kernel(WalkArgs a) {
         if (++redraws >= kMaxRedraws) break;
         continue;
       }
-      r = mix64(ctr);
-      ctr += kGolden;
-      const double p = __dmul_rn((double)(r >> 11), 1.0 / 9007199254740992.0);
-      const int64_t du = __ldg(&a.indptr[(int64_t)u + 1]) - __ldg(&a.indptr[u]);
-      const int64_t mx = ds > du ? ds : du, mn = ds < du ? ds : du;
-      const double pa = __ddiv_rn(__dmul_rn(__ddiv_rn(1.0, (double)(ds - __ldg(&a.cn[e]))), (double)mx), (double)mn);
-      const bool trace = tanh_pos(pa) <= p;
+      bool trace = false;
+      if (a.trace) {
+        r = mix64(ctr);
+        ctr += kGolden;
+        const double p = __dmul_rn((double)(r >> 11), 1.0 / 9007199254740992.0);
+        const int64_t du = __ldg(&a.indptr[(int64_t)u + 1]) - __ldg(&a.indptr[u]);
+        const int64_t mx = ds > du ? ds : du, mn = ds < du ? ds : du;
+        const double pa =
+            __ddiv_rn(__dmul_rn(__ddiv_rn(1.0, (double)(ds - __ldg(&a.cn[e]))), (double)mx), (double)mn);
+        trace = tanh_pos(pa) <= p;
+      }
       if (append(u)) break;
       if (trace) {
         if (append((int32_t)cur)) break;
@@ -314,7 +320,7 @@ size_t walk_scratch_bytes(int64_t walker_num) {
 // the last = total tokens).
 cudaError_t launch_info_walks_count(const int64_t* indptr, const int32_t* indices, const int32_t* cn,
                                     const double* xl, int64_t V, int64_t walker_num, int min_length,
-                                    int max_length, double r_threshold, uint64_t seed, void* scratch,
+                                    int max_length, double r_threshold, uint64_t seed, int trace, void* scratch,
                                     int num_sms, int64_t** offsets_out, cudaStream_t s) {
   char* p = static_cast<char*>(scratch);
   int64_t* offsets = reinterpret_cast<int64_t*>(p);
@@ -323,8 +329,8 @@ cudaError_t launch_info_walks_count(const int64_t* indptr, const int32_t* indice
   int64_t* tile_sums = reinterpret_cast<int64_t*>(p);
   p += sizeof(int64_t) * (size_t)(tiles + 1);
   int32_t* lengths = reinterpret_cast<int32_t*>(p);
-  WalkArgs a{indptr, indices, cn, xl, V, walker_num, min_length, max_length, r_threshold, seed, lengths, nullptr,
-             nullptr};
+  WalkArgs a{indptr, indices, cn, xl, V, walker_num, min_length, max_length, r_threshold, seed, trace, lengths,
+             nullptr, nullptr};
   const int T = walk_block_threads(max_length);
   const size_t smem = sizeof(int32_t) * (size_t)T * max_length;
   cudaError_t e = cudaFuncSetAttribute(info_walk_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -349,10 +355,10 @@ cudaError_t launch_info_walks_count(const int64_t* indptr, const int32_t* indice
 // Pass 2: the walks again, written at their offsets.
 cudaError_t launch_info_walks_emit(const int64_t* indptr, const int32_t* indices, const int32_t* cn,
                                    const double* xl, int64_t V, int64_t walker_num, int min_length, int max_length,
-                                   double r_threshold, uint64_t seed, const int64_t* offsets, int32_t* corpus,
-                                   int num_sms, cudaStream_t s) {
-  WalkArgs a{indptr, indices, cn, xl, V, walker_num, min_length, max_length, r_threshold, seed, nullptr, offsets,
-             corpus};
+                                   double r_threshold, uint64_t seed, int trace, const int64_t* offsets,
+                                   int32_t* corpus, int num_sms, cudaStream_t s) {
+  WalkArgs a{indptr, indices, cn, xl, V, walker_num, min_length, max_length, r_threshold, seed, trace, nullptr,
+             offsets, corpus};
   const int T = walk_block_threads(max_length);
   const size_t smem = sizeof(int32_t) * (size_t)T * max_length;
   int per_sm = 0;

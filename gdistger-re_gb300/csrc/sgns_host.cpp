@@ -1032,10 +1032,20 @@ sgns_status sgns_get_embeddings(sgns_handle* h, int32_t which, float* out) {
   const size_t n = (size_t)h->V * h->opt.size;
   const void* src = which ? h->woh : h->wih;
   if (h->opt.storage == SGNS_STORE_BF16_SR) {
-    std::vector<uint16_t> tmp(n);
-    CU(h, cudaMemcpyAsync(tmp.data(), src, n * 2, cudaMemcpyDeviceToHost, h->stream));
-    CU(h, cudaStreamSynchronize(h->stream));
-    for (size_t i = 0; i < n; i++) out[i] = bf16_bits_to_f32(tmp[i]);
+    // widened on the device in chunks through a small staging buffer, so the host receives
+    // fp32 rows directly (no host-side conversion of V*d elements)
+    const size_t chunk = std::min<size_t>(n, (size_t)8 << 20);
+    float* stage = nullptr;
+    CU(h, cudaMalloc(&stage, chunk * 4));
+    cudaError_t e = cudaSuccess;
+    for (size_t i = 0; i < n && e == cudaSuccess; i += chunk) {
+      const size_t m = std::min(chunk, n - i);
+      e = launch_widen_bf16(static_cast<const uint16_t*>(src) + i, stage, (int64_t)m, h->stream);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(out + i, stage, m * 4, cudaMemcpyDeviceToHost, h->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(stage);
+    if (e != cudaSuccess) return fail(h, SGNS_ECUDA, "reading embeddings: %s", cudaGetErrorString(e));
   } else {
     CU(h, cudaMemcpyAsync(out, src, n * 4, cudaMemcpyDeviceToHost, h->stream));
     CU(h, cudaStreamSynchronize(h->stream));
@@ -1271,6 +1281,32 @@ sgns_status sgns_minibatch_update(int32_t d, int32_t n, const int32_t* in_count,
   return SGNS_OK;
 }
 
+sgns_status sgns_minibatch_update_bf16(int32_t d, int32_t n, const int32_t* in_count, const int32_t* in_first,
+                                       const int32_t* out_count, const int32_t* out_meta, const float* alpha,
+                                       const float* in_rows, const float* out_rows, uint16_t* new_in,
+                                       uint16_t* new_out, uint64_t sr_seed, void* stream) {
+  if (d < 4 || d > kDMax || d % 4 || n < 0) return fail(nullptr, SGNS_EINVAL, "bad minibatch arguments");
+  if (n == 0) return SGNS_OK;
+  DeviceScratch* ds = device_scratch();
+  if (!ds) return fail(nullptr, SGNS_ECUDA, "no current CUDA device");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  std::lock_guard<std::mutex> g(ds->mx);
+  sgns_status st = ds->ensure(sizeof(int64_t) * 2 * n + 16);
+  if (st) return st;
+  int32_t* status = reinterpret_cast<int32_t*>(static_cast<char*>(ds->buf) + sizeof(int64_t) * 2 * n);
+  if (cudaMemsetAsync(status, 0, sizeof(int32_t), s) != cudaSuccess) return fail(nullptr, SGNS_ECUDA, "memset");
+  cudaError_t e = launch_minibatch_bf16(d, n, kIMax, in_count, in_first, out_count, out_meta, alpha, in_rows,
+                                        out_rows, new_in, new_out, sr_seed, ds->exp,
+                                        static_cast<int64_t*>(ds->buf), status, s);
+  if (e != cudaSuccess) return fail(nullptr, SGNS_ECUDA, "minibatch kernel: %s", cudaGetErrorString(e));
+  int32_t hs = 0;
+  if ((e = cudaMemcpyAsync(&hs, status, sizeof hs, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    return fail(nullptr, SGNS_ECUDA, "minibatch kernel: %s", cudaGetErrorString(e));
+  if (hs) return fail(nullptr, SGNS_EINVAL, "a minibatch exceeds %d inputs / %d outputs or has first > inputs", kIMax, kOMax);
+  return SGNS_OK;
+}
+
 sgns_status sgns_link_scores(int32_t dtype, int32_t d, const void* table, int64_t V, const int32_t* pairs,
                              int64_t n, float* scores, void* stream) {
   if ((dtype != 0 && dtype != 1) || d < 4 || d > kDMax || d % 4 || V < 1 || n < 0 ||
@@ -1356,8 +1392,9 @@ sgns_status sgns_info_walks(const sgns_walk_options* o, const int64_t* indptr, c
       cap < 0 || (cap > 0 && !corpus))
     return fail(nullptr, SGNS_EINVAL, "bad walk arguments");
   if (o->walker_num < 0 || o->min_length < 0 || o->max_length < 1 || o->max_length > kWalkMaxLength ||
-      !(o->r_threshold == o->r_threshold))
-    return fail(nullptr, SGNS_EINVAL, "walk options: walker_num >= 0, min_length >= 0, max_length in [1, %d]",
+      !(o->r_threshold == o->r_threshold) || (o->trace_steps != 0 && o->trace_steps != 1))
+    return fail(nullptr, SGNS_EINVAL,
+                "walk options: walker_num >= 0, min_length >= 0, max_length in [1, %d], trace_steps 0 or 1",
                 kWalkMaxLength);
   *n_tokens = 0;
   if (o->walker_num == 0) return SGNS_OK;
@@ -1382,7 +1419,8 @@ sgns_status sgns_info_walks(const sgns_walk_options* o, const int64_t* indptr, c
   cudaError_t e;
   if ((e = cudaMemcpyAsync(xl, hxl.data(), xl_bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
       (e = launch_info_walks_count(indptr, indices, cn, xl, V, o->walker_num, o->min_length, o->max_length,
-                                   o->r_threshold, o->seed, scratch, sms, &offsets, s)) != cudaSuccess ||
+                                   o->r_threshold, o->seed, o->trace_steps, scratch, sms, &offsets, s)) !=
+          cudaSuccess ||
       (e = cudaMemcpyAsync(&total, offsets + o->walker_num, sizeof total, cudaMemcpyDeviceToHost, s)) !=
           cudaSuccess ||
       (e = cudaStreamSynchronize(s)) != cudaSuccess)
@@ -1393,7 +1431,7 @@ sgns_status sgns_info_walks(const sgns_walk_options* o, const int64_t* indptr, c
     return fail(nullptr, SGNS_EINVAL, "walks yield %lld tokens, capacity %lld", (long long)total, (long long)cap);
   }
   if ((e = launch_info_walks_emit(indptr, indices, cn, xl, V, o->walker_num, o->min_length, o->max_length,
-                                  o->r_threshold, o->seed, offsets, corpus, sms, s)) != cudaSuccess ||
+                                  o->r_threshold, o->seed, o->trace_steps, offsets, corpus, sms, s)) != cudaSuccess ||
       (e = cudaStreamSynchronize(s)) != cudaSuccess)
     return fail(nullptr, SGNS_ECUDA, "walks: %s", cudaGetErrorString(e));
   return SGNS_OK;

@@ -160,6 +160,8 @@ cudaError_t launch_init_wih(void* wih, int storage, int64_t V, int32_t d, const 
 cudaError_t launch_map_corpus(const int32_t* ids, const int32_t* row_of, int32_t* rows, int64_t n,
                               int64_t V, int32_t* bad, cudaStream_t s);
 // longest run of non-separator tokens, capped at kMaxSentence (atomicMax into *out)
+// bf16 bits -> fp32 for n elements (n % 4 == 0)
+cudaError_t launch_widen_bf16(const void* src, float* dst, int64_t n, cudaStream_t s);
 cudaError_t launch_max_walk(const int32_t* rows, int64_t n, int32_t* out, cudaStream_t s);
 size_t window_smem_bytes(int d, int window, int K, int lmax, int warps_per_cta);
 cudaError_t window_engine_occupancy(int storage, int d, int window, int K, int lmax, int wpc,
@@ -174,6 +176,13 @@ cudaError_t launch_minibatch(int d, int n, int imax, int omax, const int32_t* in
                              const float* alpha, const float* in_rows, const float* out_rows, float* d_in,
                              float* d_out, const float* exp_table, int64_t* offsets, int32_t* status,
                              cudaStream_t s);
+// the same update, each updated row written as bf16 bits with the trainers' stochastic
+// rounding (event keys from sr_seed and the minibatch index)
+cudaError_t launch_minibatch_bf16(int d, int n, int imax, const int32_t* in_count, const int32_t* in_first,
+                                  const int32_t* out_count, const int32_t* out_meta, const float* alpha,
+                                  const float* in_rows, const float* out_rows, uint16_t* new_in, uint16_t* new_out,
+                                  uint64_t sr_seed, const float* exp_table, int64_t* offsets, int32_t* status,
+                                  cudaStream_t s);
 // host helpers shared by the translation units (sgns_host.cpp)
 // walk-file text -> corpus (dsgl_ingest.cu); scratch of ingest_scratch_bytes(n) bytes
 size_t ingest_scratch_bytes(int64_t n);
@@ -198,12 +207,12 @@ int walk_block_threads(int max_length);
 size_t walk_scratch_bytes(int64_t walker_num);
 cudaError_t launch_info_walks_count(const int64_t* indptr, const int32_t* indices, const int32_t* cn,
                                     const double* xl, int64_t V, int64_t walker_num, int min_length,
-                                    int max_length, double r_threshold, uint64_t seed, void* scratch,
+                                    int max_length, double r_threshold, uint64_t seed, int trace, void* scratch,
                                     int num_sms, int64_t** offsets_out, cudaStream_t s);
 cudaError_t launch_info_walks_emit(const int64_t* indptr, const int32_t* indices, const int32_t* cn,
                                    const double* xl, int64_t V, int64_t walker_num, int min_length, int max_length,
-                                   double r_threshold, uint64_t seed, const int64_t* offsets, int32_t* corpus,
-                                   int num_sms, cudaStream_t s);
+                                   double r_threshold, uint64_t seed, int trace, const int64_t* offsets,
+                                   int32_t* corpus, int num_sms, cudaStream_t s);
 
 void host_exp_table(float* t /* kExpTableSize + 1 */);
 int report_error(int status, const char* fmt, ...);  // sets sgns_last_error(NULL); returns status

@@ -46,7 +46,8 @@ class Stats(ctypes.Structure):
 
 class WalkOptions(ctypes.Structure):
     _fields_ = [("walker_num", ctypes.c_int64), ("min_length", ctypes.c_int32), ("max_length", ctypes.c_int32),
-                ("r_threshold", ctypes.c_double), ("seed", ctypes.c_uint64)]
+                ("r_threshold", ctypes.c_double), ("seed", ctypes.c_uint64), ("trace_steps", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 
 class SgnsError(RuntimeError):
@@ -94,6 +95,7 @@ def lib():
         L.sgns_device_tables.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp)]
         L.sgns_save_text.argtypes = [vp, ctypes.c_char_p]
         L.sgns_minibatch_update.argtypes = [i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+        L.sgns_minibatch_update_bf16.argtypes = [i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, ctypes.c_uint64, vp]
         L.sgns_minibatch_update_noalloc.argtypes = [i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
         L.sgns_parse_walks.argtypes = [vp, i64, vp, i64, ctypes.POINTER(i64), ctypes.POINTER(i64), vp]
         L.sgns_link_scores.argtypes = [i32, i32, vp, i64, vp, i64, vp, vp]
@@ -221,6 +223,10 @@ class Trainer:
         _check(lib().sgns_get_embeddings(self.h, which, _ptr(out)), self.h)
         return out
 
+    def embeddings_to(self, which, ptr):
+        """sgns_get_embeddings into caller memory at ptr (V * d floats, e.g. a pinned buffer)."""
+        _check(lib().sgns_get_embeddings(self.h, which, ctypes.c_void_p(ptr)), self.h)
+
     def set_embeddings(self, which, values):
         values = np.ascontiguousarray(values, dtype=np.float32)
         _check(lib().sgns_set_embeddings(self.h, which, _ptr(values)), self.h)
@@ -242,6 +248,17 @@ def minibatch_update(d, in_count, in_first, out_count, out_meta, alpha, in_rows,
                                        out_meta.data_ptr(), alpha.data_ptr(), in_rows.data_ptr(),
                                        out_rows.data_ptr(), d_in.data_ptr(), d_out.data_ptr(),
                                        ctypes.c_void_p(stream)))
+
+
+def minibatch_update_bf16(d, in_count, in_first, out_count, out_meta, alpha, in_rows, out_rows, new_in, new_out,
+                          seed, stream=0):
+    """sgns_minibatch_update_bf16: the update plus the BF16 trainers' rounded write-back;
+    new_in / new_out are int16 (bf16 bits) CUDA tensors shaped like in_rows / out_rows."""
+    n = int(in_count.numel())
+    _check(lib().sgns_minibatch_update_bf16(d, n, in_count.data_ptr(), in_first.data_ptr(), out_count.data_ptr(),
+                                            out_meta.data_ptr(), alpha.data_ptr(), in_rows.data_ptr(),
+                                            out_rows.data_ptr(), new_in.data_ptr(), new_out.data_ptr(), int(seed),
+                                            ctypes.c_void_p(stream)))
 
 
 def minibatch_update_noalloc(d, in_count, in_first, out_count, out_meta, alpha, in_rows, out_rows, d_in,
@@ -306,14 +323,14 @@ def edge_common_neighbors(indptr, indices, cn, stream=0):
 
 
 def info_walks(indptr, indices, cn, walker_num, min_length=20, max_length=80, r_threshold=0.999, seed=1,
-               corpus=None, stream=0):
+               corpus=None, stream=0, trace=1):
     """sgns_info_walks on device tensors.  corpus: int32 device tensor to fill (None: a new
     one of the exact size, after a counting call).  Returns (corpus, n_tokens)."""
     import torch
 
     V, E = int(indptr.numel()) - 1, int(indices.numel())
     o = WalkOptions(walker_num=int(walker_num), min_length=int(min_length), max_length=int(max_length),
-                    r_threshold=float(r_threshold), seed=int(seed))
+                    r_threshold=float(r_threshold), seed=int(seed), trace_steps=int(trace))
     n = ctypes.c_int64()
     args = (indptr.data_ptr(), indices.data_ptr() if E else None, cn.data_ptr() if E else None, V, E)
     if corpus is None:

@@ -176,6 +176,19 @@ sgns_status sgns_minibatch_update(int32_t d, int32_t n_batches, const int32_t* i
                                   const float* in_rows, const float* out_rows, float* d_in,
                                   float* d_out, void* stream);
 
+/* sgns_minibatch_update followed by the write-back of the BF16 trainers: every updated row
+ * (input row j + its update, output row i + outputMd row i) is stored as bf16 bits with
+ * their stochastic rounding (cvt.rs.bf16x2 fed by the counter hash of sr_seed, the
+ * minibatch index and the row's index within it).  The per-minibatch error of BF16 storage
+ * against an FP64 step is measured on these rows.  in_rows/out_rows: fp32 values (pass
+ * widened bf16 rows to continue from a BF16 table); new_in/new_out: uint16 bf16 bits, laid
+ * out like in_rows/out_rows.  Ordered on stream; returns after the rows are written. */
+sgns_status sgns_minibatch_update_bf16(int32_t d, int32_t n_batches, const int32_t* in_count,
+                                       const int32_t* in_first, const int32_t* out_count,
+                                       const int32_t* out_meta, const float* alpha, const float* in_rows,
+                                       const float* out_rows, uint16_t* new_in, uint16_t* new_out,
+                                       uint64_t sr_seed, void* stream);
+
 /* sgns_minibatch_update without any device allocation.  No counterpart in the
  * reference: it exists for callers that cannot let a library allocate device memory --
  * a process whose GPU memory belongs to its own allocator (a framework's caching
@@ -226,6 +239,11 @@ typedef struct sgns_walk_options {
   double r_threshold;  /* R of walk.hpp:24 (0.999): a walk stops once R*R < r_threshold or
                           R < 0 (walk.hpp:868-874) */
   uint64_t seed;       /* the walkers' random streams (counter-based; see below) */
+  int32_t trace_steps; /* 1: the reference's trace step -- a move to a neighbour with few
+                          common neighbours is followed by a return to the current vertex
+                          (walk.hpp:920-1031); 0: every move goes on to the drawn neighbour,
+                          with the same stop rule */
+  int32_t reserved;    /* 0 */
 } sgns_walk_options;
 
 /* DistGER's information-oriented walks (InCoM, include/walk.hpp:818-1042: uniform neighbour

@@ -66,8 +66,8 @@ def lib():
         L.oracle_tanh_pos.restype = ctypes.c_double
         L.oracle_edge_common_neighbors.argtypes = [vp, vp, i64, vp]
         L.oracle_edge_common_neighbors.restype = None
-        L.oracle_info_walks.argtypes = [vp, vp, vp, i64, i64, i32, i32, ctypes.c_double, ctypes.c_uint64, vp, i64,
-                                        ctypes.POINTER(i64), vp]
+        L.oracle_info_walks.argtypes = [vp, vp, vp, i64, i64, i32, i32, ctypes.c_double, ctypes.c_uint64, i32, vp,
+                                        i64, ctypes.POINTER(i64), vp]
         L.oracle_info_walks.restype = i32
         _lib = L
     return _lib
@@ -202,7 +202,7 @@ def edge_common_neighbors(indptr, indices):
     return cn
 
 
-def info_walks(indptr, indices, cn, walker_num, min_length=20, max_length=80, r_threshold=0.999, seed=1):
+def info_walks(indptr, indices, cn, walker_num, min_length=20, max_length=80, r_threshold=0.999, seed=1, trace=1):
     """Information-oriented walks restated (walk_oracle.cpp).  Returns (corpus int32 with
     -1 after each walk, lengths int32 per walker)."""
     indptr = np.ascontiguousarray(indptr, dtype=np.int64)
@@ -213,10 +213,10 @@ def info_walks(indptr, indices, cn, walker_num, min_length=20, max_length=80, r_
     lengths = np.zeros(max(walker_num, 1), np.int32)
     ie = _p(indices) if len(indices) else None
     ce = _p(cn) if len(cn) else None
-    lib().oracle_info_walks(_p(indptr), ie, ce, V, walker_num, min_length, max_length, r_threshold, seed, None, 0,
+    lib().oracle_info_walks(_p(indptr), ie, ce, V, walker_num, min_length, max_length, r_threshold, seed, trace, None, 0,
                             ctypes.byref(n), _p(lengths))
     out = np.zeros(max(n.value, 1), np.int32)
-    rc = lib().oracle_info_walks(_p(indptr), ie, ce, V, walker_num, min_length, max_length, r_threshold, seed,
+    rc = lib().oracle_info_walks(_p(indptr), ie, ce, V, walker_num, min_length, max_length, r_threshold, seed, trace,
                                  _p(out), len(out), ctypes.byref(n), None)
     assert rc == 0
     return out[:n.value], lengths[:walker_num]

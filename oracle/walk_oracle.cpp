@@ -29,7 +29,8 @@
 //   * p = uniform(draw); pa = ((1 / (ds - cn)) * max(ds, du)) / min(ds, du) with cn the
 //     edge's common-neighbour count; trace = tanh(pa) <= p;
 //   * append u (stop test), then, on a trace, append c again (stop test); the walk moves
-//     to u only without a trace.
+//     to u only without a trace.  With trace steps off (trace = 0) there is no p draw and
+//     every move goes on to u.
 // Each appended vertex updates the correlation state with f = the vertex's earlier visits
 // in this walk (Correlation::iterate, step 1), and the walk stops once it has made more
 // than min_length moves and R * R < r_threshold or R < 0 (walk.hpp:868-874), or once it
@@ -158,6 +159,7 @@ struct WalkParams {
   double r_threshold;
   uint64_t seed;
   const double* xl;
+  int32_t trace;  // 1: the trace step; 0: moves only (no p draw)
 };
 
 // One walk; writes its vertices to out (capacity max_length) and returns the count.
@@ -201,11 +203,14 @@ int walk_one(const WalkParams& P, int64_t w, int32_t* out) {
       if (++redraws >= kMaxRedraws) break;
       continue;
     }
-    const double p = (double)(draw() >> 11) * (1.0 / 9007199254740992.0);
-    const int64_t du = P.indptr[(int64_t)u + 1] - P.indptr[u];
-    const int64_t mx = ds > du ? ds : du, mn = ds < du ? ds : du;
-    const double pa = ((1.0 / (double)(ds - P.cn[e])) * (double)mx) / (double)mn;
-    const bool trace = tanh_pos(pa) <= p;
+    bool trace = false;
+    if (P.trace) {
+      const double p = (double)(draw() >> 11) * (1.0 / 9007199254740992.0);
+      const int64_t du = P.indptr[(int64_t)u + 1] - P.indptr[u];
+      const int64_t mx = ds > du ? ds : du, mn = ds < du ? ds : du;
+      const double pa = ((1.0 / (double)(ds - P.cn[e])) * (double)mx) / (double)mn;
+      trace = tanh_pos(pa) <= p;
+    }
     if (append(u)) break;
     if (trace) {
       if (append((int32_t)cur)) break;
@@ -252,10 +257,11 @@ void oracle_edge_common_neighbors(const int64_t* indptr, const int32_t* indices,
 // the walks yield (also when cap is too small: then nothing is written and 1 returned).
 int32_t oracle_info_walks(const int64_t* indptr, const int32_t* indices, const int32_t* cn, int64_t V,
                           int64_t walker_num, int32_t min_length, int32_t max_length, double r_threshold,
-                          uint64_t seed, int32_t* corpus, int64_t cap, int64_t* n_tokens, int32_t* lengths) {
+                          uint64_t seed, int32_t trace, int32_t* corpus, int64_t cap, int64_t* n_tokens,
+                          int32_t* lengths) {
   std::vector<double> xl((size_t)max_length + 2);
   oracle_xlog2x_table(max_length + 2, xl.data());
-  WalkParams P{indptr, indices, cn, V, min_length, max_length, r_threshold, seed, xl.data()};
+  WalkParams P{indptr, indices, cn, V, min_length, max_length, r_threshold, seed, xl.data(), trace};
   const int64_t n = walker_num;
   std::vector<int32_t> len((size_t)n);
 #pragma omp parallel

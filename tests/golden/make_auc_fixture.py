@@ -3,9 +3,17 @@ engines' AUC is compared with (bench.py's auc_sbm leg, tests/test_gpu_auc.py).
 
 The survey's configuration 2: a 4-block stochastic block model (p_in / p_out = 20, about
 2.73 undirected edges per vertex), 10% of the edges held out as in src/tools/gtrain.cpp
-:293-333, 10 information-oriented walks per vertex (the rule of include/walk.hpp:818-1042,
-min length 20, capped at 80 vertices, R threshold 0.78 for a mean length near 40),
-d = 128, window 10, 5 negatives, sample 1e-3, alpha 0.01, one pass, unigram table 1e8.
+:293-333, 10 information-oriented walks per vertex (the entropy/length stop rule of
+include/walk.hpp:260-387, 868-874, min length 20, capped at 80 vertices, R threshold 0.84
+for a mean length near 40), d = 128, window 10, 5 negatives, sample 1e-3, alpha 0.01, one
+pass, unigram table 1e8.
+
+The walks make no trace steps (sgns_walk_options.trace_steps = 0).  On this graph nearly
+no edge has a common neighbour, so the reference's trace step returns to the current
+vertex on about 80% of the moves; walks then cover only a few hops and the one-pass
+training links held-out edges barely better than chance (AUC 0.54 for the CPU trainer and
+for the reference's own trainer on one seed, recorded under "trace_walks"), which cannot
+tell engines apart.  Without trace steps the same stop rule gives AUC near 0.78.
 
 Everything is drawn on the CPU from fixed seeds with platform-independent integer
 arithmetic (synth.sbm_csr, synth.holdout_csr, the oracle's walker), so the GPU side can
@@ -35,7 +43,9 @@ OUT = os.path.join(ROOT, "tests", "golden", "auc_sbm.json")
 REF_BIN = os.path.join(ROOT, "oracle", "_ref", "dsgl_ref")
 
 GRAPH = dict(edges_per_vertex=2.73, blocks=4, ratio=20.0, holdout=0.1)
-WALKS = dict(walks_per_vertex=10, min_length=20, max_length=80, r_threshold=0.78)
+WALKS = dict(walks_per_vertex=10, min_length=20, max_length=80, r_threshold=0.84, trace_steps=0)
+# the reference's trace steps on the same graph (one recorded case; see above)
+TRACE_WALKS = dict(walks_per_vertex=10, min_length=20, max_length=80, r_threshold=0.78, trace_steps=1)
 TRAIN = dict(size=128, window=10, negative=5, sample=1e-3, alpha=0.01, iter=1, table_size=100_000_000,
              table_threads=12)
 
@@ -49,7 +59,7 @@ def sha(a):
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
-def build_case(V, seed):
+def build_case(V, seed, walks=WALKS):
     """(train_indptr, train_indices, pos, neg, corpus, info) of one case, on the CPU."""
     import oracle
     import synth
@@ -58,8 +68,8 @@ def build_case(V, seed):
     ip, ix, _ = synth.sbm_csr(V, int(GRAPH["edges_per_vertex"] * V), GRAPH["blocks"], GRAPH["ratio"], seed=s["graph"])
     tip, tix, pos, neg = synth.holdout_csr(ip, ix, GRAPH["holdout"], seed=s["holdout"])
     cn = oracle.edge_common_neighbors(tip, tix)
-    corpus, lengths = oracle.info_walks(tip, tix, cn, WALKS["walks_per_vertex"] * V, WALKS["min_length"],
-                                        WALKS["max_length"], WALKS["r_threshold"], s["walks"])
+    corpus, lengths = oracle.info_walks(tip, tix, cn, walks["walks_per_vertex"] * V, walks["min_length"],
+                                        walks["max_length"], walks["r_threshold"], s["walks"], walks["trace_steps"])
     info = dict(V=V, seed=seed, seeds=s, edges=int(len(ix) // 2), train_edges=int(len(tix) // 2),
                 holdout=int(pos.shape[1]), tokens=int(len(corpus)), walk_mean_length=float(lengths.mean()),
                 graph_sha256=sha(np.concatenate([tip.view(np.int32), tix])), pos_sha256=sha(pos),
@@ -118,9 +128,19 @@ def main():
     ap.add_argument("--threads", type=int, default=8)
     ap.add_argument("--reference-seed", type=int, default=1)
     ap.add_argument("--reference-vertices", type=int, nargs="*", default=[100_000])
+    ap.add_argument("--trace-case", action="store_true", help="also record the trace-step walks at 100k, seed 1")
     args = ap.parse_args()
     data = json.load(open(OUT)) if os.path.exists(OUT) else {}
     data.update(graph=GRAPH, walks=WALKS, train=TRAIN, generator=os.path.relpath(__file__, ROOT))
+    if "trace_walks" not in data and args.trace_case:
+        tip, tix, pos, neg, corpus, info = build_case(100_000, 1, TRACE_WALKS)
+        info["walks"] = TRACE_WALKS
+        info["cpu_trainer"] = cpu_trainer(corpus, 100_000, pos, neg, args.threads)
+        if os.path.exists(REF_BIN):
+            info["reference"] = reference_trainer(corpus, 100_000, pos, neg, args.threads)
+        data["trace_walks"] = info
+        with open(OUT, "w") as f:
+            json.dump(data, f, indent=1)
     cases = {(c["V"], c["seed"]): c for c in data.get("cases", [])}
     for V in args.vertices:
         for seed in args.seeds:

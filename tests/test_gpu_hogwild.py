@@ -1,0 +1,68 @@
+"""Many workers at once (Hogwild), checked row by row.
+
+The reference's compute threads update shared tables without locks (dsgl.hpp:1352-1356,
+1380-1404); which update wins a race is not reproducible, so per-row parity needs workers
+whose rows do not meet.  The corpus here is one connected component per worker, each laid
+out so that a worker's contiguous slice (dsgl.hpp:811-826) is exactly its component's walks,
+with no negatives (-negative 0: the outputs are the two walks' targets) and fewer than
+10,000 tokens per worker (no learning-rate update, which sums all workers' progress,
+dsgl.hpp:886-897).  Every row is then written by one worker only, so the GPU engines, with
+all workers in flight at once, must give the oracle's rows at the same worker count: the
+survey's per-row tolerance under Hogwild ordering is 1e-5 relative, and here the order of
+each row's updates is fixed, so the rows are required bit for bit."""
+import numpy as np
+import pytest
+
+from test_gpu_parity import gpu_train, oracle_train
+
+pytestmark = pytest.mark.gpu
+
+
+def component_corpus(workers, verts_per_comp, tokens_per_worker, seed):
+    """workers components of verts_per_comp vertices (ids offset per component), each a ring
+    with random chords; uniform random walks filling exactly tokens_per_worker tokens per
+    component (separators included), in component order."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(workers):
+        base = k * verts_per_comp
+        n = verts_per_comp
+        nb = [[(i + 1) % n, (i - 1) % n] for i in range(n)]
+        for _ in range(2 * n):
+            a, b = rng.integers(0, n, 2)
+            if a != b:
+                nb[a].append(int(b))
+                nb[b].append(int(a))
+        toks = []
+        while len(toks) < tokens_per_worker:
+            room = tokens_per_worker - len(toks)
+            if room < 3:  # pad the last walk instead of leaving a too-short remainder
+                toks[-1:-1] = [toks[-2]] * room
+                break
+            L = int(min(rng.integers(5, 60), room - 1))
+            v = int(rng.integers(0, n))
+            for _ in range(L):
+                toks.append(base + v)
+                v = nb[v][int(rng.integers(0, len(nb[v])))]
+            toks.append(-1)
+        assert len(toks) == tokens_per_worker
+        out += toks
+    return np.array(out, np.int32)
+
+
+@pytest.mark.parametrize("engine,storage", [("plain", "fp32"), ("persistent", "fp32"), ("persistent", "bf16")])
+def test_disjoint_workers_match_the_oracle_row_for_row(engine, storage, sgns_lib, oracle_mod):
+    W, n, T = 48, 400, 9000
+    corpus = component_corpus(W, n, T, seed=17)
+    cfg = dict(V=W * n, d=64, window=5, negative=0, iter=1, sample=1e-3, alpha=0.025)
+    wih, woh, st, _ = gpu_train(cfg, corpus, engine, storage, workers=W, wpc=4)
+    policy = oracle_mod.POLICY_REF if engine == "plain" else oracle_mod.POLICY_WINDOW
+    owih, owoh, ost = oracle_train(oracle_mod, cfg, corpus, policy, storage, workers=W)
+    assert st.workers == W
+    assert (st.steps, st.pairs, st.word_count_actual) == (ost["steps"], ost["pairs"], ost["word_count_actual"])
+    rel = np.linalg.norm(wih - owih, axis=1) / np.maximum(np.linalg.norm(owih, axis=1), 1e-30)
+    assert rel.max() <= 1e-5, rel.max()
+    assert np.array_equal(wih.view(np.uint32), owih.view(np.uint32))
+    assert np.array_equal(woh.view(np.uint32), owoh.view(np.uint32))
+    # the rows did move: the test is not passing on untrained tables
+    assert np.abs(woh).max() > 0

@@ -83,3 +83,99 @@ def test_minibatch_error_vs_fp64(sgns_lib, oracle_mod):
     # sigma-table cell crossings are rare; all other rows are within 1e-5
     assert flips <= 0.02 * len(errs), flips
     assert np.median(errs) < 1e-6
+
+
+M64 = (1 << 64) - 1
+
+
+def mix64(z):
+    z = (z + 0x9E3779B97F4A7C15) & M64
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M64
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M64
+    return z ^ (z >> 31)
+
+
+def sr_rows(v, seed, kind, b):
+    """The trainers' write-back rule on fp32 rows v [rows, d]: column 4q + j of row r takes
+    bits [16j, 16j + 16) of mix64(key ^ (r << 8) ^ q), key = mix64(seed ^ (kind << 56) ^ b);
+    stored bits = (bits(x) + r16) >> 16."""
+    key = mix64((seed ^ (kind << 56) ^ b) & M64)
+    u = v.astype(np.float32).view(np.uint32).astype(np.uint64)
+    out = np.zeros(v.shape, np.uint16)
+    for r in range(v.shape[0]):
+        for q in range(v.shape[1] // 4):
+            bits = mix64(key ^ ((r << 8) & M64) ^ q)
+            for j in range(4):
+                r16 = (bits >> (16 * j)) & 0xFFFF
+                out[r, 4 * q + j] = (int(u[r, 4 * q + j]) + r16) >> 16
+    return out
+
+
+def run_gpu_bf16(batches, d, seed):
+    import torch
+
+    dev = "cuda"
+    in_count = torch.tensor([b[0].shape[0] for b in batches], dtype=torch.int32, device=dev)
+    in_first = torch.tensor([b[3] for b in batches], dtype=torch.int32, device=dev)
+    out_count = torch.tensor([b[1].shape[0] for b in batches], dtype=torch.int32, device=dev)
+    meta = torch.tensor(np.concatenate([b[2] for b in batches]), device=dev)
+    alpha = torch.tensor([b[4] for b in batches], dtype=torch.float32, device=dev)
+    xin = torch.tensor(np.concatenate([b[0] for b in batches]), device=dev)
+    xout = torch.tensor(np.concatenate([b[1] for b in batches]), device=dev)
+    n_in = torch.full(xin.shape, 0x7FC1, dtype=torch.int16, device=dev)
+    n_out = torch.full(xout.shape, 0x7FC1, dtype=torch.int16, device=dev)
+    sgns.minibatch_update_bf16(d, in_count, in_first, out_count, meta, alpha, xin, xout, n_in, n_out, seed)
+    torch.cuda.synchronize()
+    return n_in.cpu().numpy().view(np.uint16), n_out.cpu().numpy().view(np.uint16)
+
+
+def bf16_values(batches):
+    """The same minibatches with every row rounded to a bf16 value (a BF16 table's rows)."""
+    r = lambda a: ((a.view(np.uint32) + 0x8000) & 0xFFFF0000).view(np.float32)
+    return [(r(x), r(o), m, f, a) for x, o, m, f, a in batches]
+
+
+@pytest.mark.parametrize("d", [16, 128, 256])
+def test_bf16_writeback_is_the_trainers_rounding(d, sgns_lib):
+    """sgns_minibatch_update_bf16 stores row + update (the fp32 update of
+    sgns_minibatch_update, added in fp32) with the trainers' stochastic-rounding rule."""
+    batches = bf16_values(random_minibatches(40, d, seed=100 + d))
+    gi, go = run_gpu(batches, d)
+    bi, bo = run_gpu_bf16(batches, d, seed=77)
+    oi = oo = 0
+    for b, (xin, xout, meta, first, alpha) in enumerate(batches):
+        I, O = xin.shape[0], xout.shape[0]
+        exp_in = sr_rows(xin + gi[oi:oi + I], 77, 2, b)    # inputs: event kind 2 (walk rows)
+        exp_out = sr_rows(xout + go[oo:oo + O], 77, 4, b)  # outputs: event kind 4 (negatives)
+        assert np.array_equal(bi[oi:oi + I], exp_in), b
+        assert np.array_equal(bo[oo:oo + O], exp_out), b
+        oi += I
+        oo += O
+
+
+def test_bf16_per_minibatch_error_vs_fp64(sgns_lib, oracle_mod):
+    """Configuration 3's error statement at test size: 1000 minibatches from bf16 rows, each
+    row's stored bf16 value against the fp64 step.  Stochastic rounding moves an element by
+    less than one bf16 unit in the last place (2^-7 of its magnitude or less), so no row's
+    relative error can exceed 2^-7; it is unbiased, so the mean signed error is near 0 ulp."""
+    d = 128
+    batches = bf16_values(random_minibatches(1000, d, seed=6))
+    bi, bo = run_gpu_bf16(batches, d, seed=5)
+    widen = lambda u: (u.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+    ri, ro = widen(bi), widen(bo)
+    oi = oo = 0
+    errs, ulps = [], []
+    for xin, xout, meta, first, alpha in batches:
+        dIn, dOut = oracle_mod.minibatch(xin, xout, meta, first, float(alpha), acc64=True)
+        I, O = xin.shape[0], xout.shape[0]
+        for stored, base, upd in ((ri[oi:oi + I], xin, dIn), (ro[oo:oo + O], xout, dOut)):
+            new64 = base.astype(np.float64) + upd
+            errs.append(np.max(np.linalg.norm(stored - new64, axis=1) / np.maximum(np.linalg.norm(new64, axis=1), 1e-30)))
+            nz = new64 != 0
+            ulps.append(np.mean((stored[nz] - new64[nz]) / 2.0 ** (np.floor(np.log2(np.abs(new64[nz]))) - 7)))
+        oi += I
+        oo += O
+    errs = np.array(errs)
+    assert errs.max() <= 2.0 ** -7 * 1.001, errs.max()
+    assert np.median(errs) < 4e-3, np.median(errs)
+    assert abs(np.mean(ulps)) < 0.02, np.mean(ulps)

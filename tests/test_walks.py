@@ -39,7 +39,7 @@ def python_common_neighbors(ip, ix):
     return np.array([len(nb[u] & nb[int(ix[e])]) for u in range(V) for e in range(ip[u], ip[u + 1])], np.int32)
 
 
-def python_walk(ip, ix, cn, xl, tanh_pos, w, min_length, max_length, r_th, seed):
+def python_walk(ip, ix, cn, xl, tanh_pos, w, min_length, max_length, r_th, seed, trace=1):
     """The walker rule as a plain loop (the oracle's arithmetic primitives, small graphs)."""
     M = (1 << 64) - 1
     G = 0x9E3779B97F4A7C15
@@ -110,13 +110,15 @@ def python_walk(ip, ix, cn, xl, tanh_pos, w, min_length, max_length, r_th, seed)
             if redraws >= 64:
                 break
             continue
-        p = float(draw() >> 11) * (1.0 / 9007199254740992.0)
-        du = int(ip[u + 1] - ip[u])
-        pa = ((1.0 / float(ds - int(cn[e]))) * float(max(ds, du))) / float(min(ds, du)) if ds > cn[e] else math.inf
-        trace = tanh_pos(pa) <= p
+        tr = False
+        if trace:
+            p = float(draw() >> 11) * (1.0 / 9007199254740992.0)
+            du = int(ip[u + 1] - ip[u])
+            pa = ((1.0 / float(ds - int(cn[e]))) * float(max(ds, du))) / float(min(ds, du)) if ds > cn[e] else math.inf
+            tr = tanh_pos(pa) <= p
         if append(u):
             break
-        if trace:
+        if tr:
             if append(cur):
                 break
         else:
@@ -145,22 +147,23 @@ def test_oracle_common_neighbors_are_set_intersections(oracle_mod):
         assert np.array_equal(oracle_mod.edge_common_neighbors(ip, ix), python_common_neighbors(ip, ix)), name
 
 
-@pytest.mark.parametrize("min_length,max_length,r_th,seed", [(20, 80, 0.999, 1), (20, 80, 0.8, 2), (0, 30, 0.95, 3),
-                                                             (5, 1, 0.9, 4), (3, 1000, 0.5, 5)])
-def test_oracle_walks_follow_the_rule(oracle_mod, min_length, max_length, r_th, seed):
+@pytest.mark.parametrize("min_length,max_length,r_th,seed,trace", [(20, 80, 0.999, 1, 1), (20, 80, 0.8, 2, 1),
+                                                                   (0, 30, 0.95, 3, 1), (5, 1, 0.9, 4, 1),
+                                                                   (3, 1000, 0.5, 5, 1), (20, 80, 0.84, 6, 0)])
+def test_oracle_walks_follow_the_rule(oracle_mod, min_length, max_length, r_th, seed, trace):
     """The restated walker against the rule written as a plain loop, walk by walk."""
     xl = oracle_mod.xlog2x_table(1002)
     for name, ip, ix in small_graphs():
         cn = oracle_mod.edge_common_neighbors(ip, ix)
         V = len(ip) - 1
         n = min(3 * V, 600)
-        corpus, lengths = oracle_mod.info_walks(ip, ix, cn, n, min_length, max_length, r_th, seed)
+        corpus, lengths = oracle_mod.info_walks(ip, ix, cn, n, min_length, max_length, r_th, seed, trace)
         ends = np.flatnonzero(corpus == -1)
         assert len(ends) == n and np.array_equal(np.diff(np.concatenate([[-1], ends])) - 1, lengths)
         starts = np.concatenate([[0], ends[:-1] + 1])
         for w in range(0, n, 7 if V > 100 else 1):
             walk = corpus[starts[w]:ends[w]].tolist()
-            ref = python_walk(ip, ix, cn, xl, oracle_mod.tanh_pos, w, min_length, max_length, r_th, seed)
+            ref = python_walk(ip, ix, cn, xl, oracle_mod.tanh_pos, w, min_length, max_length, r_th, seed, trace)
             assert walk == ref, (name, w)
 
 
@@ -200,17 +203,19 @@ def test_gpu_common_neighbors_match_oracle(sgns_lib, oracle_mod):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("min_length,max_length,r_th,seed", [(20, 80, 0.999, 1), (20, 80, 0.78, 2), (0, 30, 0.95, 3),
-                                                             (5, 1, 0.9, 4), (3, 1000, 0.5, 5), (20, 200, 0.7, 6)])
-def test_gpu_walks_match_oracle(sgns_lib, oracle_mod, min_length, max_length, r_th, seed):
+@pytest.mark.parametrize("min_length,max_length,r_th,seed,trace", [(20, 80, 0.999, 1, 1), (20, 80, 0.78, 2, 1),
+                                                                   (0, 30, 0.95, 3, 1), (5, 1, 0.9, 4, 1),
+                                                                   (3, 1000, 0.5, 5, 1), (20, 200, 0.7, 6, 1),
+                                                                   (20, 80, 0.84, 7, 0), (0, 1000, 0.6, 8, 0)])
+def test_gpu_walks_match_oracle(sgns_lib, oracle_mod, min_length, max_length, r_th, seed, trace):
     import torch
 
     for name, ip, ix in small_graphs():
         cn = oracle_mod.edge_common_neighbors(ip, ix)
         n = 5 * (len(ip) - 1) + 3
-        ref, _ = oracle_mod.info_walks(ip, ix, cn, n, min_length, max_length, r_th, seed)
+        ref, _ = oracle_mod.info_walks(ip, ix, cn, n, min_length, max_length, r_th, seed, trace)
         dip, dix, dcn = (torch.from_numpy(a).cuda() for a in (ip, ix, cn))
-        out, n_tok = sgns.info_walks(dip, dix, dcn, n, min_length, max_length, r_th, seed)
+        out, n_tok = sgns.info_walks(dip, dix, dcn, n, min_length, max_length, r_th, seed, trace=trace)
         assert n_tok == len(ref) and np.array_equal(out.cpu().numpy(), ref), (name, n_tok, len(ref))
 
 
@@ -226,9 +231,10 @@ def test_gpu_walks_at_scale_match_oracle(sgns_lib, oracle_mod):
     dcn = torch.empty(len(tix), dtype=torch.int32, device="cuda")
     sgns.edge_common_neighbors(dip, dix, dcn)
     assert np.array_equal(dcn.cpu().numpy(), cn)
-    ref, _ = oracle_mod.info_walks(tip, tix, cn, 400_000, 20, 80, 0.78, 10)
-    out, n_tok = sgns.info_walks(dip, dix, dcn, 400_000, 20, 80, 0.78, 10)
-    assert n_tok == len(ref) and np.array_equal(out.cpu().numpy(), ref)
+    for trace, r_th in ((1, 0.78), (0, 0.84)):
+        ref, _ = oracle_mod.info_walks(tip, tix, cn, 400_000, 20, 80, r_th, 10, trace)
+        out, n_tok = sgns.info_walks(dip, dix, dcn, 400_000, 20, 80, r_th, 10, trace=trace)
+        assert n_tok == len(ref) and np.array_equal(out.cpu().numpy(), ref), trace
 
 
 @pytest.mark.gpu
@@ -260,6 +266,9 @@ def test_gpu_walk_arguments_are_checked(sgns_lib):
         sgns.edge_common_neighbors(torch.tensor([0, 2, 3, 4], dtype=torch.int64, device="cuda"),
                                    torch.tensor([2, 1, 0, 0], dtype=torch.int32, device="cuda"),
                                    torch.zeros(4, dtype=torch.int32, device="cuda"))
+    assert e.value.status == sgns.EINVAL
+    with pytest.raises(sgns.SgnsError) as e:
+        sgns.info_walks(ip, ix, cn, 4, 0, 5, 0.9, 1, trace=2)
     assert e.value.status == sgns.EINVAL
     for kw in (dict(max_length=0), dict(max_length=1001), dict(min_length=-1)):
         args = dict(min_length=0, max_length=5)
