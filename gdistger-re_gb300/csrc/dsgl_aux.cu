@@ -2,6 +2,8 @@
 // minibatch update, and the SGNS loss with its hand-written adjoint.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "dsgl_device.cuh"
 
 namespace sgns {
@@ -185,6 +187,55 @@ __global__ void widen_bf16_kernel(const uint2* __restrict__ src, float4* __restr
     dst[i] = make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xFFFF0000u), __uint_as_float(u.y << 16),
                          __uint_as_float(u.y & 0xFFFF0000u));
   }
+}
+
+// ---- hotness-block sync: rows out of and back into a table (one warp per row) ----------
+__global__ void gather_rows_kernel(const void* tab, int storage, int d, const int32_t* rows, int64_t n, float* buf) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+    const int64_t r = rows[i];
+    for (int c = lane; c < d; c += 32)
+      buf[i * d + c] = storage == STORE_BF16 ? bf16_bits_to_f32(static_cast<const uint16_t*>(tab)[r * d + c])
+                                             : static_cast<const float*>(tab)[r * d + c];
+  }
+}
+// row = buf / divisor (fp32 division, as the reference averages, dsgl.hpp:741-745); bf16
+// tables round to nearest even, so every rank stores the same bits
+__global__ void scatter_rows_kernel(void* tab, int storage, int d, const int32_t* rows, int64_t n, const float* buf,
+                                    float divisor) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+    const int64_t r = rows[i];
+    for (int c = lane; c < d; c += 32) {
+      const float v = __fdiv_rn(buf[i * d + c], divisor);
+      if (storage == STORE_BF16) {
+        const uint32_t u = __float_as_uint(v);
+        uint16_t b;
+        if ((u & 0x7F800000u) == 0x7F800000u) b = (uint16_t)((u >> 16) | ((u & 0xFFFFu) ? 0x40u : 0u));
+        else b = (uint16_t)((u + 0x7FFFu + ((u >> 16) & 1u)) >> 16);
+        static_cast<uint16_t*>(tab)[r * d + c] = b;
+      } else {
+        static_cast<float*>(tab)[r * d + c] = v;
+      }
+    }
+  }
+}
+
+cudaError_t launch_gather_rows(const void* tab, int storage, int d, const int32_t* rows, int64_t n, float* buf,
+                               cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  const int64_t blocks = std::min<int64_t>((n + 7) / 8, 152 * 16);
+  gather_rows_kernel<<<(unsigned)blocks, 256, 0, s>>>(tab, storage, d, rows, n, buf);
+  return cudaGetLastError();
+}
+cudaError_t launch_scatter_rows(void* tab, int storage, int d, const int32_t* rows, int64_t n, const float* buf,
+                                float divisor, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  const int64_t blocks = std::min<int64_t>((n + 7) / 8, 152 * 16);
+  scatter_rows_kernel<<<(unsigned)blocks, 256, 0, s>>>(tab, storage, d, rows, n, buf, divisor);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_widen_bf16(const void* src, float* dst, int64_t n, cudaStream_t s) {

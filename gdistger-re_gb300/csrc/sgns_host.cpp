@@ -1082,6 +1082,64 @@ sgns_status sgns_device_tables(sgns_handle* h, void** wih, void** woh) {
   return SGNS_OK;
 }
 
+sgns_status sgns_sync_rows(const sgns_handle* h, uint64_t seed, uint64_t round, int32_t full, int32_t* rows,
+                           int64_t cap, int64_t* n_rows) {
+  if (!h || !n_rows || cap < 0 || (cap > 0 && !rows)) return fail(nullptr, SGNS_EINVAL, "bad sync-row arguments");
+  if (h->V == 0) return fail(nullptr, SGNS_ESTATE, "sgns_set_vocab has not been called");
+  const int32_t st = sgns_internal_sync_rows(h->cn_sorted.data(), h->V, seed, round, full, rows, cap, n_rows);
+  if (st) return fail(nullptr, SGNS_EINVAL, "%lld sync rows, capacity %lld", (long long)*n_rows, (long long)cap);
+  return SGNS_OK;
+}
+
+// The row draw of sgns_sync_rows from the count-sorted counts; exported for the CPU tests.
+int32_t sgns_internal_sync_rows(const int32_t* cn_sorted, int64_t V, uint64_t seed, uint64_t round, int32_t full,
+                                int32_t* rows, int64_t cap, int64_t* n_rows) {
+  std::vector<int32_t> out;
+  if (full) {
+    out.resize(V);
+    for (int64_t r = 0; r < V; r++) out[r] = (int32_t)r;
+  } else {
+    // block starts: row 0 and every row whose count differs from the previous row's
+    std::vector<int64_t> starts{0};
+    for (int64_t r = 1; r < V; r++)
+      if (cn_sorted[r] != cn_sorted[r - 1]) starts.push_back(r);
+    // one row per block [starts[j-1], starts[j]) for j = 1..: the last block is not drawn
+    const uint64_t base = mix64(seed ^ (round * 0x9E3779B97F4A7C15ULL));
+    for (size_t j = 1; j < starts.size(); j++) {
+      const uint64_t r = mix64(base + (uint64_t)j * 0x9E3779B97F4A7C15ULL);
+      const uint64_t len = (uint64_t)(starts[j] - starts[j - 1]);
+      out.push_back((int32_t)(starts[j - 1] + (int64_t)(((r >> 32) * len) >> 32)));
+    }
+  }
+  *n_rows = (int64_t)out.size();
+  if ((int64_t)out.size() > cap) return SGNS_EINVAL;
+  if (!out.empty()) memcpy(rows, out.data(), sizeof(int32_t) * out.size());
+  return SGNS_OK;
+}
+
+sgns_status sgns_gather_rows(sgns_handle* h, int32_t which, const int32_t* rows, int64_t n, float* buf) {
+  if (!h || (which != 0 && which != 1) || n < 0 || (n > 0 && (!rows || !buf)))
+    return fail(h, SGNS_EINVAL, "bad gather arguments");
+  if (!h->wih) return fail(h, SGNS_ESTATE, "sgns_set_vocab has not been called");
+  CU(h, cudaSetDevice(h->opt.device));
+  CU(h, launch_gather_rows(which ? h->woh : h->wih, h->opt.storage == SGNS_STORE_BF16_SR ? STORE_BF16 : STORE_F32,
+                           h->opt.size, rows, n, buf, h->stream));
+  CU(h, cudaStreamSynchronize(h->stream));
+  return SGNS_OK;
+}
+
+sgns_status sgns_scatter_rows(sgns_handle* h, int32_t which, const int32_t* rows, int64_t n, const float* buf,
+                              float divisor) {
+  if (!h || (which != 0 && which != 1) || n < 0 || (n > 0 && (!rows || !buf)) || !(divisor > 0))
+    return fail(h, SGNS_EINVAL, "bad scatter arguments");
+  if (!h->wih) return fail(h, SGNS_ESTATE, "sgns_set_vocab has not been called");
+  CU(h, cudaSetDevice(h->opt.device));
+  CU(h, launch_scatter_rows(which ? h->woh : h->wih, h->opt.storage == SGNS_STORE_BF16_SR ? STORE_BF16 : STORE_F32,
+                            h->opt.size, rows, n, buf, divisor, h->stream));
+  CU(h, cudaStreamSynchronize(h->stream));
+  return SGNS_OK;
+}
+
 sgns_status sgns_save_text(sgns_handle* h, const char* path) {
   NvtxRange r_("sgns_save_text");
   if (!h || !path) return fail(h, SGNS_EINVAL, "bad arguments");
@@ -1445,37 +1503,30 @@ sgns_status sgns_loss_adjoint(int32_t dtype, int32_t d, int64_t V, int32_t n, co
   if (dtype < 0 || dtype > 2 || d < 1 || d > kDMax || V < 1 || V > INT32_MAX || n < 0 || !n_in || !n_out)
     return fail(nullptr, SGNS_EINVAL, "bad adjoint arguments");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  // minibatch extents (host copies of the two offset arrays)
-  std::vector<int32_t> ip(n + 1), op(n + 1);
-  cudaError_t e;
-  if ((e = cudaMemcpyAsync(ip.data(), in_ptr, sizeof(int32_t) * (n + 1), cudaMemcpyDeviceToHost, s)) ||
-      (e = cudaMemcpyAsync(op.data(), out_ptr, sizeof(int32_t) * (n + 1), cudaMemcpyDeviceToHost, s)) ||
-      (e = cudaStreamSynchronize(s)))
-    return fail(nullptr, SGNS_ECUDA, "adjoint: %s", cudaGetErrorString(e));
-  int imax = 1, omax = 1;
-  for (int b = 0; b < n; b++) {
-    const int I = ip[b + 1] - ip[b], O = op[b + 1] - op[b];
-    if (I < 0 || O < 0) return fail(nullptr, SGNS_EINVAL, "adjoint: offsets not ascending at batch %d", b);
-    imax = std::max(imax, I);
-    omax = std::max(omax, O);
-  }
-  if (imax > kIMax || omax > kOMax)
-    return fail(nullptr, SGNS_EINVAL, "adjoint: a minibatch exceeds %d inputs / %d outputs", kIMax, kOMax);
   DeviceScratch* ds = device_scratch();
   if (!ds) return fail(nullptr, SGNS_ECUDA, "no current CUDA device");
   std::lock_guard<std::mutex> g(ds->mx);
   sgns_status st = ds->ensure(adjoint_scratch_bytes(V) + 64);
   if (st) return st;
-  int32_t* nu = reinterpret_cast<int32_t*>(static_cast<char*>(ds->buf) + adjoint_scratch_bytes(V));
-  e = launch_adjoint(dtype, d, n, V, ip[n], op[n], in_ptr, in_ids, in_first, out_ptr, out_ids, out_meta, wih, woh,
-                     loss, grad_in_ids, grad_in, grad_out_ids, grad_out, nu, ds->buf, imax, omax, s);
+  int32_t* info = reinterpret_cast<int32_t*>(static_cast<char*>(ds->buf) + adjoint_scratch_bytes(V));
+  // phase 1 finds, on the device, the distinct rows and the largest minibatch; its sizes
+  // (five ints) are the one read-back before the gradient kernel
+  cudaError_t e = launch_adjoint_prepare(dtype, d, n, V, in_ptr, in_ids, in_first, out_ptr, out_ids, loss,
+                                         grad_in_ids, grad_in, grad_out_ids, grad_out, info, ds->buf, s);
+  int32_t h[5];
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, info, sizeof h, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return fail(nullptr, SGNS_ECUDA, "adjoint: %s", cudaGetErrorString(e));
+  if (h[2] & 2)
+    return fail(nullptr, SGNS_EINVAL, "adjoint: a minibatch has descending or negative offsets, more than %d inputs "
+                "or %d outputs, or first outside [0, inputs]", kIMax, kOMax);
+  if (h[2] & 1) return fail(nullptr, SGNS_EINVAL, "adjoint: a row id outside [0, %lld)", (long long)V);
+  *n_in = h[0];
+  *n_out = h[1];
+  e = launch_adjoint(dtype, d, n, V, h[3], h[4], in_ptr, in_ids, in_first, out_ptr, out_ids, out_meta, wih, woh, loss,
+                     grad_in, grad_out, ds->buf, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return fail(nullptr, SGNS_ECUDA, "adjoint kernels: %s", cudaGetErrorString(e));
-  int32_t h3[3];
-  if ((e = cudaMemcpyAsync(h3, nu, sizeof h3, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s)))
-    return fail(nullptr, SGNS_ECUDA, "adjoint: %s", cudaGetErrorString(e));
-  if (h3[2]) return fail(nullptr, SGNS_EINVAL, "adjoint: a row id outside [0, %lld)", (long long)V);
-  *n_in = h3[0];
-  *n_out = h3[1];
   return SGNS_OK;
 }
 

@@ -160,6 +160,12 @@ cudaError_t launch_init_wih(void* wih, int storage, int64_t V, int32_t d, const 
 cudaError_t launch_map_corpus(const int32_t* ids, const int32_t* row_of, int32_t* rows, int64_t n,
                               int64_t V, int32_t* bad, cudaStream_t s);
 // longest run of non-separator tokens, capped at kMaxSentence (atomicMax into *out)
+// hotness-block sync: rows of a table (fp32 or bf16) to fp32 rows of buf and back
+// (table row = buf row / divisor, bf16 rounded to nearest even)
+cudaError_t launch_gather_rows(const void* tab, int storage, int d, const int32_t* rows, int64_t n, float* buf,
+                               cudaStream_t s);
+cudaError_t launch_scatter_rows(void* tab, int storage, int d, const int32_t* rows, int64_t n, const float* buf,
+                                float divisor, cudaStream_t s);
 // bf16 bits -> fp32 for n elements (n % 4 == 0)
 cudaError_t launch_widen_bf16(const void* src, float* dst, int64_t n, cudaStream_t s);
 cudaError_t launch_max_walk(const int32_t* rows, int64_t n, int32_t* out, cudaStream_t s);
@@ -218,12 +224,18 @@ void host_exp_table(float* t /* kExpTableSize + 1 */);
 int report_error(int status, const char* fmt, ...);  // sets sgns_last_error(NULL); returns status
 
 size_t adjoint_scratch_bytes(int64_t V);
-cudaError_t launch_adjoint(int dtype, int d, int n, int64_t V, int64_t total_in, int64_t total_out,
-                           const int32_t* in_ptr, const int32_t* in_ids, const int32_t* in_first,
-                           const int32_t* out_ptr, const int32_t* out_ids, const int32_t* out_meta,
-                           const void* wih, const void* woh, double* loss, int32_t* grad_in_ids, void* grad_in,
-                           int32_t* grad_out_ids, void* grad_out, int32_t* n_unique, void* scratch,
-                           int imax, int omax, cudaStream_t s);
+// phase 1 of the adjoint: marks, checks, slots, ids, zeroed gradient rows; info (device, 5
+// ints): distinct input rows, distinct output rows, status bits (1 bad id, 2 bad size),
+// largest input count, largest output count
+cudaError_t launch_adjoint_prepare(int dtype, int d, int n, int64_t V, const int32_t* in_ptr, const int32_t* in_ids,
+                                   const int32_t* in_first, const int32_t* out_ptr, const int32_t* out_ids,
+                                   double* loss, int32_t* grad_in_ids, void* grad_in, int32_t* grad_out_ids,
+                                   void* grad_out, int32_t* info, void* scratch, cudaStream_t s);
+// phase 2: loss and row gradients (imax / omax from phase 1)
+cudaError_t launch_adjoint(int dtype, int d, int n, int64_t V, int imax, int omax, const int32_t* in_ptr,
+                           const int32_t* in_ids, const int32_t* in_first, const int32_t* out_ptr,
+                           const int32_t* out_ids, const int32_t* out_meta, const void* wih, const void* woh,
+                           double* loss, void* grad_in, void* grad_out, void* scratch, cudaStream_t s);
 
 }  // namespace sgns
 
@@ -241,3 +253,7 @@ extern "C" int32_t sgns_internal_write_embedding(const uint32_t* order, const fl
 // The walker's x * log2(x) table (n entries) exactly as sgns_info_walks builds it; exported
 // for the CPU tests.
 extern "C" void sgns_internal_xlog2x_table(int32_t n, double* t);
+// The row draw of sgns_sync_rows from count-sorted counts (no device); exported for the CPU
+// tests.  Returns SGNS_EINVAL (with *n_rows set) when cap is too small.
+extern "C" int32_t sgns_internal_sync_rows(const int32_t* cn_sorted, int64_t V, uint64_t seed, uint64_t round,
+                                           int32_t full, int32_t* rows, int64_t cap, int64_t* n_rows);

@@ -109,6 +109,12 @@ def lib():
         L.sgns_internal_host_vocab.restype = i32
         L.sgns_internal_write_embedding.argtypes = [vp, vp, i64, i32, i32, ctypes.c_char_p]
         L.sgns_internal_write_embedding.restype = i32
+        L.sgns_sync_rows.argtypes = [vp, ctypes.c_uint64, ctypes.c_uint64, i32, vp, i64, ctypes.POINTER(i64)]
+        L.sgns_gather_rows.argtypes = [vp, i32, vp, i64, vp]
+        L.sgns_scatter_rows.argtypes = [vp, i32, vp, i64, vp, ctypes.c_float]
+        L.sgns_internal_sync_rows.argtypes = [vp, i64, ctypes.c_uint64, ctypes.c_uint64, i32, vp, i64,
+                                              ctypes.POINTER(i64)]
+        L.sgns_internal_sync_rows.restype = i32
         L.sgns_internal_xlog2x_table.argtypes = [i32, vp]
         L.sgns_internal_xlog2x_table.restype = None
         for name in header_functions():  # every declared entry point must be exported
@@ -239,6 +245,41 @@ class Trainer:
     def save_text(self, path):
         _check(lib().sgns_save_text(self.h, path.encode()), self.h)
 
+    def sync_rows(self, seed, round, full=False):
+        """sgns_sync_rows: the rows of one hotness-block sync round (int32, host)."""
+        out = np.zeros(max(self.vocab_size, 1), np.int32)
+        n = ctypes.c_int64()
+        _check(lib().sgns_sync_rows(self.h, seed, round, int(full), _ptr(out), len(out), ctypes.byref(n)))
+        return out[:n.value]
+
+    def gather_rows(self, which, rows, buf):
+        """rows: int32 CUDA tensor; buf: float32 CUDA tensor [n, d] (filled)."""
+        _check(lib().sgns_gather_rows(self.h, which, rows.data_ptr(), int(rows.numel()), buf.data_ptr()), self.h)
+
+    def scatter_rows(self, which, rows, buf, divisor):
+        _check(lib().sgns_scatter_rows(self.h, which, rows.data_ptr(), int(rows.numel()), buf.data_ptr(),
+                                       float(divisor)), self.h)
+
+    def sync_hot_rows(self, seed, round, full=False, group=None):
+        """One round of the hotness-block sync across the replicas of a torch.distributed
+        group (dsgl.hpp:641-756): the round's rows of Wih and Woh, summed over the replicas
+        by all_reduce, divided by the replica count."""
+        import torch
+        import torch.distributed as dist
+
+        rows = torch.from_numpy(self.sync_rows(seed, round, full)).cuda(self.opt.device)
+        world = dist.get_world_size(group)
+        bufs = {}
+
+        def gather(which, r):
+            bufs[which] = torch.empty((r.numel(), self.opt.size), dtype=torch.float32, device=r.device)
+            self.gather_rows(which, r, bufs[which])
+            return bufs[which]
+
+        hot_row_sync(rows, gather, lambda which, r, b, w: self.scatter_rows(which, r, b, w), world,
+                     lambda b: dist.all_reduce(b, op=dist.ReduceOp.SUM, group=group))
+        return int(rows.numel())
+
 
 def minibatch_update(d, in_count, in_first, out_count, out_meta, alpha, in_rows, out_rows, d_in, d_out,
                      stream=0):
@@ -339,6 +380,27 @@ def info_walks(indptr, indices, cn, walker_num, min_length=20, max_length=80, r_
     _check(lib().sgns_info_walks(ctypes.byref(o), *args, corpus.data_ptr(), int(corpus.numel()), ctypes.byref(n),
                                  ctypes.c_void_p(stream)))
     return corpus[:n.value], n.value
+
+
+def hot_row_sync(rows, gather, scatter, world, all_reduce):
+    """The exchange of one hotness-block sync round (dsgl.hpp:731-755), for any transport:
+    for Wih then Woh, gather(which, rows) -> rows as an fp32 buffer, all_reduce(buffer)
+    sums it over the replicas in place, scatter(which, rows, buffer, world) stores
+    buffer / world back."""
+    for which in (0, 1):
+        buf = gather(which, rows)
+        all_reduce(buf)
+        scatter(which, rows, buf, float(world))
+
+
+def internal_sync_rows(cn_sorted, seed, round, full=False):
+    """The row draw of sgns_sync_rows from count-sorted counts, on the host (no device)."""
+    cn_sorted = np.ascontiguousarray(cn_sorted, dtype=np.int32)
+    out = np.zeros(max(len(cn_sorted), 1), np.int32)
+    n = ctypes.c_int64()
+    _check(lib().sgns_internal_sync_rows(_ptr(cn_sorted), len(cn_sorted), seed, round, int(full), _ptr(out), len(out),
+                                         ctypes.byref(n)))
+    return out[:n.value]
 
 
 def host_vocab(counts, sample, table_size, threads):

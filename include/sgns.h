@@ -159,6 +159,29 @@ sgns_status sgns_get_embeddings(sgns_handle* h, int32_t which, float* out);
 sgns_status sgns_set_embeddings(sgns_handle* h, int32_t which, const float* in);
 /* Device pointers of Wih/Woh (fp32 or bf16 elements, sorted-row order). */
 sgns_status sgns_device_tables(sgns_handle* h, void** wih, void** woh);
+/* ---- hotness-block model sync between replicas (dsgl.hpp:548-781) ---------------------
+ * Data-parallel replicas (one per GPU, each training its own walks) average a sample of
+ * rows every sync period: rows sorted by count fall into blocks of equal count
+ * (word_freq_block, dsgl.hpp:493-509); one row is drawn per block -- every block but the
+ * last, as the reference's loop does (dsgl.hpp:645-711) -- and those rows of Wih and Woh
+ * are summed over the replicas (MPI_Allreduce, dsgl.hpp:739-740) and divided by the replica
+ * count (:741-746).  The library provides the row draw and the device gather / scatter;
+ * the caller's collective (NCCL, MPI, torch.distributed) sums the gathered rows.
+ *
+ * sgns_sync_rows: the rows of one sync round, drawn from a counter-based stream of (seed,
+ * round) so every replica draws the same rows (the reference broadcasts rank 0's draw,
+ * :724-729); full = 1 gives every row (the reference's full sync, :602-630).  rows: host
+ * output of capacity cap (V is enough); *n_rows: the count. */
+sgns_status sgns_sync_rows(const sgns_handle* h, uint64_t seed, uint64_t round, int32_t full, int32_t* rows,
+                           int64_t cap, int64_t* n_rows);
+/* Rows rows[0..n) (device) of Wih (which = 0) or Woh (1) into buf (device, n x d fp32),
+ * ordered on the handle's stream; returns when buf is written. */
+sgns_status sgns_gather_rows(sgns_handle* h, int32_t which, const int32_t* rows, int64_t n, float* buf);
+/* The reverse: table row rows[i] = buf[i] / divisor (fp32 division; bf16 tables round to
+ * nearest even, so every replica stores identical bits). */
+sgns_status sgns_scatter_rows(sgns_handle* h, int32_t which, const int32_t* rows, int64_t n, const float* buf,
+                              float divisor);
+
 /* my_saveModel (dsgl.hpp:1443-1461): "V d\n" then "<id> " + d x "%f " + "\n" per row. */
 sgns_status sgns_save_text(sgns_handle* h, const char* path);
 
