@@ -536,7 +536,8 @@ def run_sweep(args):
                     t.upload(c[:cut])
                     ps = t.train()
                 rows.append({"d": d, "K": K, "storage": sto, "persistent_pairs_per_s": st.pairs / st.train_ms * 1e3,
-                             "warps_per_cta": st.warps_per_cta, "workers": st.workers,
+                             "warps_per_cta": st.warps_per_cta, "forward_tile": st.forward_tile,
+                             "warps_per_worker": st.warps_per_worker, "workers": st.workers,
                              "persistent_roofline": _row_roofline(st),
                              "plain_pairs_per_s": ps.pairs / ps.train_ms * 1e3, "plain_roofline": _row_roofline(ps),
                              "speedup": (st.pairs / st.train_ms) / (ps.pairs / ps.train_ms)})
@@ -853,7 +854,8 @@ def main():
                                    (args.workload, wl["V"], edges, wl["gamma"], wl["walks"], wl["mean"], wl["cap"],
                                     n_tok),
                        "engine": "persistent", "storage": "bf16-sr", "workers": st_last.workers,
-                       "warps_per_cta": st_last.warps_per_cta, "l2": "inputs larger than L2 (no flush)",
+                       "warps_per_cta": st_last.warps_per_cta, "forward_tile": st_last.forward_tile,
+                       "warps_per_worker": st_last.warps_per_worker, "l2": "inputs larger than L2 (no flush)",
                        "parallelism": "replicas x%d" % ws, **TRAIN},
             "roofline": roofline, "gpu_launches": args.steps, "clocks": clk,
             "steps_per_launch": st_last.steps, "pairs_per_launch": st_last.pairs, "corpus_gen_s": gen_s}

@@ -118,7 +118,9 @@ __device__ __forceinline__ void store_row_from_smem(void* tab, int64_t row, int 
 // into the step.  DFIX: the hidden size as a compile-time constant (0: read from p.d).  With
 // d known, every shared-memory address of the step is a base register plus an immediate
 // offset and the column-range guards vanish; the arithmetic is the same either way.
-template <int S, int DCH, int OM, bool kLoss, int DFIX>
+// TILE: lanes per input in the forward dot products (2: two lanes share an input while at
+// most 16 inputs remain; the same bits), chosen by the autotuner.
+template <int S, int DCH, int OM, bool kLoss, int DFIX, int TILE>
 __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
   extern __shared__ __align__(16) float smem[];
   float* exp_s = smem;
@@ -390,9 +392,9 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     __syncwarp();
     const float alpha = *reinterpret_cast<volatile float*>(&p.ctr->alpha);
     auto in_ptr = [&](int j) -> const float* { return rows + (size_t)in_row[j] * DP; };
-    // two lanes per input for small rounds pays for fp32 tables with d <= 128, K <= 5 (the
-    // other variants have no registers to spare)
-    if (S == STORE_F32 && DCH == 1 && OM == 7)
+    // two lanes per input for small rounds (d <= 128, K <= 5 only: the other variants have
+    // no registers to spare)
+    if (TILE == 2 && DCH == 1 && OM == 7)
       forward_gradient_two_lanes<OM>(I, I0, O, d, in_ptr, out_rows, DP, out_meta, exp_s, alpha, corrP, kLoss, loss);
     else
       forward_gradient_split8<OM>(I, I0, O, d, in_ptr, out_rows, DP, out_meta, exp_s, alpha, corrP,
@@ -528,48 +530,60 @@ inline int fixed_d(int d) {
   return 0;
 }
 
-template <int S, int DCH, int OM, bool kLoss, int DFIX>
+template <int S, int DCH, int OM, bool kLoss, int DFIX, int TILE>
 static cudaError_t occupancy_d(int d, int w, int K, int lmax, int wpc, int* ctas) {
   const size_t smem = window_smem_bytes(d, w, K, lmax, wpc);
-  cudaError_t e = cudaFuncSetAttribute(window_engine_kernel<S, DCH, OM, kLoss, DFIX>,
+  cudaError_t e = cudaFuncSetAttribute(window_engine_kernel<S, DCH, OM, kLoss, DFIX, TILE>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas, window_engine_kernel<S, DCH, OM, kLoss, DFIX>, 32 * wpc,
-                                                       smem);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas, window_engine_kernel<S, DCH, OM, kLoss, DFIX, TILE>,
+                                                       32 * wpc, smem);
+}
+template <int S, int DCH, int OM, int DFIX>
+static cudaError_t occupancy_tile(int d, int w, int K, int lmax, int wpc, int tile, int* ctas) {
+  if constexpr (DCH == 1 && OM == 7)
+    if (tile == 2) return occupancy_d<S, DCH, OM, false, DFIX, 2>(d, w, K, lmax, wpc, ctas);
+  return occupancy_d<S, DCH, OM, false, DFIX, 1>(d, w, K, lmax, wpc, ctas);
 }
 template <int S, int DCH, int OM>
-static cudaError_t occupancy_t(int d, int w, int K, int lmax, int wpc, int* ctas) {
+static cudaError_t occupancy_t(int d, int w, int K, int lmax, int wpc, int tile, int* ctas) {
   const int f = fixed_d(d);
   if constexpr (DCH == 1) {
-    if (f == 64) return occupancy_d<S, DCH, OM, false, 64>(d, w, K, lmax, wpc, ctas);
-    if (f == 128) return occupancy_d<S, DCH, OM, false, 128>(d, w, K, lmax, wpc, ctas);
+    if (f == 64) return occupancy_tile<S, DCH, OM, 64>(d, w, K, lmax, wpc, tile, ctas);
+    if (f == 128) return occupancy_tile<S, DCH, OM, 128>(d, w, K, lmax, wpc, tile, ctas);
   } else {
-    if (f == 256) return occupancy_d<S, DCH, OM, false, 256>(d, w, K, lmax, wpc, ctas);
+    if (f == 256) return occupancy_tile<S, DCH, OM, 256>(d, w, K, lmax, wpc, tile, ctas);
   }
-  return occupancy_d<S, DCH, OM, false, 0>(d, w, K, lmax, wpc, ctas);
+  return occupancy_tile<S, DCH, OM, 0>(d, w, K, lmax, wpc, tile, ctas);
 }
 
-template <int S, int DCH, int OM, bool kLoss, int DFIX>
+template <int S, int DCH, int OM, bool kLoss, int DFIX, int TILE>
 static cudaError_t launch_loss_t(const TrainParams& p, int wpc, cudaStream_t s) {
   const size_t smem = window_smem_bytes(p.d, p.window, p.K, p.lmax, wpc);
-  cudaError_t e = cudaFuncSetAttribute(window_engine_kernel<S, DCH, OM, kLoss, DFIX>,
+  cudaError_t e = cudaFuncSetAttribute(window_engine_kernel<S, DCH, OM, kLoss, DFIX, TILE>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const int blocks = (p.workers + wpc - 1) / wpc;
-  window_engine_kernel<S, DCH, OM, kLoss, DFIX><<<blocks, 32 * wpc, smem, s>>>(p);
+  window_engine_kernel<S, DCH, OM, kLoss, DFIX, TILE><<<blocks, 32 * wpc, smem, s>>>(p);
   return cudaGetLastError();
+}
+template <int S, int DCH, int OM, bool kLoss, int DFIX>
+static cudaError_t launch_tile_t(const TrainParams& p, int wpc, cudaStream_t s) {
+  if constexpr (DCH == 1 && OM == 7)
+    if (p.fwd_tile == 2) return launch_loss_t<S, DCH, OM, kLoss, DFIX, 2>(p, wpc, s);
+  return launch_loss_t<S, DCH, OM, kLoss, DFIX, 1>(p, wpc, s);
 }
 template <int S, int DCH, int OM>
 static cudaError_t launch_t(const TrainParams& p, int wpc, cudaStream_t s) {
-  if (p.compute_loss) return launch_loss_t<S, DCH, OM, true, 0>(p, wpc, s);
+  if (p.compute_loss) return launch_tile_t<S, DCH, OM, true, 0>(p, wpc, s);
   const int f = fixed_d(p.d);
   if constexpr (DCH == 1) {
-    if (f == 64) return launch_loss_t<S, DCH, OM, false, 64>(p, wpc, s);
-    if (f == 128) return launch_loss_t<S, DCH, OM, false, 128>(p, wpc, s);
+    if (f == 64) return launch_tile_t<S, DCH, OM, false, 64>(p, wpc, s);
+    if (f == 128) return launch_tile_t<S, DCH, OM, false, 128>(p, wpc, s);
   } else {
-    if (f == 256) return launch_loss_t<S, DCH, OM, false, 256>(p, wpc, s);
+    if (f == 256) return launch_tile_t<S, DCH, OM, false, 256>(p, wpc, s);
   }
-  return launch_loss_t<S, DCH, OM, false, 0>(p, wpc, s);
+  return launch_tile_t<S, DCH, OM, false, 0>(p, wpc, s);
 }
 
 // kernel variants: storage x column chunks per lane (d <= 128 or <= 256) x outputs per
@@ -585,8 +599,8 @@ static cudaError_t launch_t(const TrainParams& p, int wpc, cudaStream_t s) {
     return small_ ? FN<STORE_F32, 1, 7>(__VA_ARGS__) : FN<STORE_F32, 1, kOMax>(__VA_ARGS__);                \
   } while (0)
 
-cudaError_t window_engine_occupancy(int storage, int d, int w, int K, int lmax, int wpc, int* ctas) {
-  SGNS_WINDOW_DISPATCH(occupancy_t, d, w, K, lmax, wpc, ctas);
+cudaError_t window_engine_occupancy(int storage, int d, int w, int K, int lmax, int wpc, int tile, int* ctas) {
+  SGNS_WINDOW_DISPATCH(occupancy_t, d, w, K, lmax, wpc, tile, ctas);
 }
 
 cudaError_t launch_window_engine(const TrainParams& p, int wpc, cudaStream_t s) {

@@ -64,7 +64,7 @@ struct sgns_handle {
   void* plain_scratch = nullptr;
   size_t plain_bytes = 0;
   // persistent engine launch shape and its captured graph
-  int workers = 0, wpc = 0;
+  int workers = 0, wpc = 0, tile = 1;
   bool tuned = false;
   cudaGraphExec_t graph = nullptr;
   std::string graph_key;
@@ -298,6 +298,10 @@ sgns_status validate(sgns_handle* h, const sgns_options& o) {
     return fail(h, SGNS_EINVAL, "workers/warps_per_cta out of range");
   if (o.mode != SGNS_MODE_HOGWILD && o.mode != SGNS_MODE_REPLAY_EXACT)
     return fail(h, SGNS_EINVAL, "unknown mode %d", o.mode);
+  if (o.forward_tile < 0 || o.forward_tile > 2)
+    return fail(h, SGNS_EINVAL, "forward_tile %d: 0 (tuned), 1 or 2", o.forward_tile);
+  if (o.forward_tile == 2 && !window_engine_has_tile2(o.size, o.negative))
+    return fail(h, SGNS_EINVAL, "forward_tile 2 needs d <= 128 and K <= 5");
   if (o.mode == SGNS_MODE_REPLAY_EXACT && o.workers > 1)
     return fail(h, SGNS_EINVAL, "-mode exact replays one worker; -workers %d asks for more", o.workers);
   return SGNS_OK;
@@ -330,6 +334,7 @@ TrainParams make_params(sgns_handle* h, int workers) {
   p.compute_loss = o.compute_loss;
   p.lmax = h->lmax;
   p.storage = o.storage == SGNS_STORE_BF16_SR ? STORE_BF16 : STORE_F32;
+  p.fwd_tile = h->tile;
   p.ctr = h->d_ctr;
   return p;
 }
@@ -359,6 +364,8 @@ sgns_status finish_stats(sgns_handle* h, int workers, float ms) {
   s.train_ms = ms;
   s.workers = workers;
   s.warps_per_cta = h->opt.engine == SGNS_ENGINE_PERSISTENT ? h->wpc : 4;
+  s.forward_tile = h->opt.engine == SGNS_ENGINE_PERSISTENT ? h->tile : 0;
+  s.warps_per_worker = 1;
   s.row_loads = c.row_loads;
   s.row_stores = c.row_stores;
   s.output_rows = c.outputs;
@@ -370,7 +377,7 @@ sgns_status persistent_shape(sgns_handle* h, int wpc, int* workers) {
   int ctas = 0;
   const sgns_options& o = h->opt;
   CU(h, window_engine_occupancy(o.storage == SGNS_STORE_BF16_SR ? STORE_BF16 : STORE_F32, o.size,
-                                o.window, o.negative, h->lmax, wpc, &ctas));
+                                o.window, o.negative, h->lmax, wpc, h->tile, &ctas));
   if (ctas < 1)
     return fail(h, SGNS_EINVAL, "a %d-warp CTA does not fit in shared memory (d=%d, walks up to %d)", wpc,
                 o.size, h->lmax);
@@ -389,8 +396,8 @@ sgns_status run_persistent(sgns_handle* h, int workers, int wpc, bool use_graph,
   TrainParams p = make_params(h, workers);
   if (use_graph) {
     char key[256];
-    snprintf(key, sizeof key, "%p/%lld/%d/%d/%p/%p/%d/%d", (void*)h->d_corpus, (long long)h->n_tokens,
-             workers, wpc, h->wih, h->woh, h->lmax, h->opt.iter);
+    snprintf(key, sizeof key, "%p/%lld/%d/%d/%p/%p/%d/%d/%d", (void*)h->d_corpus, (long long)h->n_tokens,
+             workers, wpc, h->wih, h->woh, h->lmax, h->opt.iter, h->tile);
     if (!h->graph || h->graph_key != key) {
       if (h->graph) cudaGraphExecDestroy(h->graph);
       h->graph = nullptr;
@@ -479,49 +486,78 @@ std::string tune_key(const sgns_handle* h) {
     if (*c == '\t' || *c == '\n') *c = ' ';
   return key;
 }
-int tune_cache_lookup(const std::string& key) {
+// "key<TAB>warps_per_cta<TAB>forward_tile" lines; the last entry for a key wins
+bool tune_cache_lookup(const std::string& key, int* wpc, int* tile) {
   const char* path = getenv("SGNS_TUNE_CACHE");
-  if (!path || !*path) return 0;
+  if (!path || !*path) return false;
   FILE* f = fopen(path, "r");
-  if (!f) return 0;
+  if (!f) return false;
   char line[512];
-  int wpc = 0;
+  bool found = false;
   while (fgets(line, sizeof line, f)) {
     char* tab = strchr(line, '\t');
     if (!tab) continue;
     *tab = 0;
-    if (key == line) wpc = atoi(tab + 1);  // the last entry for a key wins
+    if (key != line) continue;
+    int a = 0, b = 1;
+    if (sscanf(tab + 1, "%d\t%d", &a, &b) >= 1 && a >= 1 && a <= 8 && (b == 1 || b == 2)) {
+      *wpc = a;
+      *tile = b;
+      found = true;
+    }
   }
   fclose(f);
-  return wpc >= 1 && wpc <= 8 ? wpc : 0;
+  return found;
 }
-void tune_cache_store(const std::string& key, int wpc) {
+void tune_cache_store(const std::string& key, int wpc, int tile) {
   const char* path = getenv("SGNS_TUNE_CACHE");
   if (!path || !*path) return;
   if (FILE* f = fopen(path, "a")) {
-    fprintf(f, "%s\t%d\n", key.c_str(), wpc);
+    fprintf(f, "%s\t%d\t%d\n", key.c_str(), wpc, tile);
     fclose(f);
   }
 }
 
+// The forward tile used when none is given and nothing is tuned: two lanes per input for
+// fp32 tables (measured faster there), one for bf16.
+int default_tile(const sgns_handle* h) {
+  if (!window_engine_has_tile2(h->opt.size, h->opt.negative)) return 1;
+  if (h->opt.forward_tile > 0) return h->opt.forward_tile;
+  return h->opt.storage == SGNS_STORE_FP32 ? 2 : 1;
+}
+
+// Autotuner: times each launch shape of the persistent engine -- warps per CTA (1..8) and,
+// where the shape has it, the forward tile (1 or 2 lanes per input) -- on a prefix of the
+// corpus, on scratch copies of the tables, and keeps the fastest (pairs per second).
+// Autotuner cache: with SGNS_TUNE_CACHE naming a file, the choice is kept per device model
+// and problem shape and reused by later runs.  The file is only an optimisation: any error
+// reading or writing it is ignored.
 sgns_status autotune(sgns_handle* h) {
   const sgns_options& o = h->opt;
   const std::string key = tune_key(h);
+  const bool tile2 = window_engine_has_tile2(o.size, o.negative);
   if (o.warps_per_cta <= 0) {
-    if (const int cached = tune_cache_lookup(key)) {
+    int cached = 0, ctile = 1;
+    if (tune_cache_lookup(key, &cached, &ctile)) {
+      if (!tile2) ctile = 1;
+      if (o.forward_tile > 0) ctile = o.forward_tile;
+      h->tile = ctile;
       int workers = o.workers;
       if (!workers && persistent_shape(h, cached, &workers) != SGNS_OK) workers = 0;
       if (workers > 0) {
         h->wpc = cached;
         h->workers = workers;
         h->tuned = true;
-        if (o.debug > 0) fprintf(stderr, "sgns: persistent engine shape from the tuning cache: %d warps/CTA\n", cached);
+        if (o.debug > 0)
+          fprintf(stderr, "sgns: persistent engine shape from the tuning cache: %d warps/CTA, tile %d\n", cached,
+                  ctile);
         return SGNS_OK;
       }
     }
   }
-  if (o.warps_per_cta > 0) {
+  if (o.warps_per_cta > 0) {  // a given CTA shape: only the tile may be left to choose
     h->wpc = o.warps_per_cta;
+    h->tile = default_tile(h);
     h->workers = o.workers;
     if (!h->workers) {
       sgns_status st = persistent_shape(h, h->wpc, &h->workers);
@@ -547,7 +583,7 @@ sgns_status autotune(sgns_handle* h) {
     dfree(woh_s);
   };
   double best = -1.0;
-  int best_wpc = 1, best_workers = 0;
+  int best_wpc = 1, best_workers = 0, best_tile = default_tile(h);
   sgns_status st = SGNS_OK;
   cudaError_t e;
   if ((e = cudaMalloc(&wih_s, tbytes)) != cudaSuccess || (e = cudaMalloc(&woh_s, tbytes)) != cudaSuccess) {
@@ -555,6 +591,7 @@ sgns_status autotune(sgns_handle* h) {
     // workers (warps per SM bound this latency-bound kernel); ties go to the wider CTA
     restore();
     cudaGetLastError();
+    h->tile = best_tile;
     for (int wpc = 1; wpc <= 8; wpc++) {
       int workers = 0;
       if (persistent_shape(h, wpc, &workers) != SGNS_OK) continue;
@@ -580,28 +617,34 @@ sgns_status autotune(sgns_handle* h) {
   h->wih = wih_s;
   h->woh = woh_s;
   h->opt.iter = 1;
-  for (int wpc = 1; wpc <= 8; wpc++) {
-    int workers = 0;
-    st = persistent_shape(h, wpc, &workers);
-    if (st) {
-      st = SGNS_OK;
-      continue;
-    }
-    if (o.workers > 0) workers = o.workers;
-    // a prefix long enough to give every worker a few hundred steps
-    h->n_tokens = std::min<int64_t>(n0, (int64_t)workers * 2000);
-    float ms = 0.f;
-    st = run_persistent(h, workers, wpc, false, &ms);
-    if (st) break;
-    if ((e = cudaMemcpy(h->h_ctr, h->d_ctr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost)) != cudaSuccess) {
-      st = fail(h, SGNS_ECUDA, "autotuner counters: %s", cudaGetErrorString(e));
-      break;
-    }
-    const double rate = ms > 0 ? (double)h->h_ctr->pairs / ms : 0.0;
-    if (rate > best) {
-      best = rate;
-      best_wpc = wpc;
-      best_workers = workers;
+  const int tile_lo = o.forward_tile > 0 ? o.forward_tile : 1;
+  const int tile_hi = o.forward_tile > 0 ? o.forward_tile : (tile2 ? 2 : 1);
+  for (int tile = tile_lo; tile <= tile_hi && !st; tile++) {
+    h->tile = tile;
+    for (int wpc = 1; wpc <= 8; wpc++) {
+      int workers = 0;
+      st = persistent_shape(h, wpc, &workers);
+      if (st) {
+        st = SGNS_OK;
+        continue;
+      }
+      if (o.workers > 0) workers = o.workers;
+      // a prefix long enough to give every worker a few hundred steps
+      h->n_tokens = std::min<int64_t>(n0, (int64_t)workers * 2000);
+      float ms = 0.f;
+      st = run_persistent(h, workers, wpc, false, &ms);
+      if (st) break;
+      if ((e = cudaMemcpy(h->h_ctr, h->d_ctr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost)) != cudaSuccess) {
+        st = fail(h, SGNS_ECUDA, "autotuner counters: %s", cudaGetErrorString(e));
+        break;
+      }
+      const double rate = ms > 0 ? (double)h->h_ctr->pairs / ms : 0.0;
+      if (rate > best) {
+        best = rate;
+        best_wpc = wpc;
+        best_workers = workers;
+        best_tile = tile;
+      }
     }
   }
   restore();
@@ -609,10 +652,12 @@ sgns_status autotune(sgns_handle* h) {
   if (best_workers == 0) return fail(h, SGNS_EINVAL, "no persistent-engine shape fits this configuration");
   h->wpc = best_wpc;
   h->workers = best_workers;
+  h->tile = best_tile;
   h->tuned = true;
-  tune_cache_store(key, best_wpc);
+  tune_cache_store(key, best_wpc, best_tile);
   if (o.debug > 0)
-    fprintf(stderr, "sgns: autotuned persistent engine: %d warps/CTA, %d workers\n", h->wpc, h->workers);
+    fprintf(stderr, "sgns: autotuned persistent engine: %d warps/CTA, tile %d, %d workers\n", h->wpc, h->tile,
+            h->workers);
   return SGNS_OK;
 }
 
@@ -732,7 +777,8 @@ sgns_status sgns_options_from_args(sgns_options* o, int argc, const char* const*
   } ints[] = {{"-size", &o->size},         {"-debug", &o->debug},         {"-binary", &o->binary},
               {"-window", &o->window},     {"-negative", &o->negative},   {"-threads", &o->threads},
               {"-iter", &o->iter},         {"-min-count", &o->min_count}, {"-batch-size", &o->batch_size},
-              {"-workers", &o->workers},   {"-warps-per-cta", &o->warps_per_cta}, {"-device", &o->device},
+              {"-workers", &o->workers},   {"-warps-per-cta", &o->warps_per_cta},
+              {"-forward-tile", &o->forward_tile}, {"-device", &o->device},
               {"-loss", &o->compute_loss}};
   for (auto& f : ints) {
     int i = pos(f.name);
@@ -972,6 +1018,7 @@ sgns_status sgns_train(sgns_handle* h) {
     if (exact) {  // one worker in a one-warp CTA: nothing to tune
       workers = 1;
       h->wpc = h->opt.warps_per_cta > 0 ? h->opt.warps_per_cta : 1;
+      h->tile = default_tile(h);
       st = run_persistent(h, 1, h->wpc, true, &ms);
       if (st) return st;
       return finish_stats(h, workers, ms);

@@ -147,7 +147,8 @@ struct TrainParams {
   int32_t d, window, K, iter, workers, sample_on;
   float start_alpha, alpha_denom;
   uint64_t sr_seed;
-  int32_t compute_loss, lmax, storage, pad;
+  int32_t compute_loss, lmax, storage;
+  int32_t fwd_tile;                // lanes per input in the forward (1, or 2 where supported)
   DeviceCounters* ctr;
   // plain-engine state (HBM)
   void* plain_state;
@@ -170,8 +171,10 @@ cudaError_t launch_scatter_rows(void* tab, int storage, int d, const int32_t* ro
 cudaError_t launch_widen_bf16(const void* src, float* dst, int64_t n, cudaStream_t s);
 cudaError_t launch_max_walk(const int32_t* rows, int64_t n, int32_t* out, cudaStream_t s);
 size_t window_smem_bytes(int d, int window, int K, int lmax, int warps_per_cta);
-cudaError_t window_engine_occupancy(int storage, int d, int window, int K, int lmax, int wpc,
+cudaError_t window_engine_occupancy(int storage, int d, int window, int K, int lmax, int wpc, int tile,
                                     int* ctas_per_sm);
+// whether a problem shape has the two-lanes-per-input forward (d <= 128, K <= 5)
+inline bool window_engine_has_tile2(int d, int K) { return d <= 128 && K <= 5; }
 cudaError_t launch_window_engine(const TrainParams& p, int warps_per_cta, cudaStream_t s);
 size_t plain_worker_bytes(int d, int window, int K, int lmax);
 cudaError_t launch_plain_init(const TrainParams& p, cudaStream_t s);

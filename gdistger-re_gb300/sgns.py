@@ -28,7 +28,8 @@ class Options(ctypes.Structure):
         ("debug", ctypes.c_int32), ("binary", ctypes.c_int32), ("storage", ctypes.c_int32),
         ("engine", ctypes.c_int32), ("workers", ctypes.c_int32), ("warps_per_cta", ctypes.c_int32),
         ("device", ctypes.c_int32), ("compute_loss", ctypes.c_int32), ("mode", ctypes.c_int32),
-        ("table_size", ctypes.c_int64), ("seed", ctypes.c_uint64),
+        ("table_size", ctypes.c_int64), ("seed", ctypes.c_uint64), ("forward_tile", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
     ]
 
 
@@ -38,6 +39,7 @@ class Stats(ctypes.Structure):
         ("row_bytes", ctypes.c_uint64), ("loss", ctypes.c_double), ("final_alpha", ctypes.c_float),
         ("train_ms", ctypes.c_float), ("workers", ctypes.c_int32), ("warps_per_cta", ctypes.c_int32),
         ("row_loads", ctypes.c_uint64), ("row_stores", ctypes.c_uint64), ("output_rows", ctypes.c_uint64),
+        ("forward_tile", ctypes.c_int32), ("warps_per_worker", ctypes.c_int32),
     ]
 
     def as_dict(self):

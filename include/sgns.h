@@ -80,6 +80,11 @@ typedef struct sgns_options {
   int32_t mode;        /* sgns_mode (-mode hogwild|exact)                         */
   int64_t table_size;  /* unigram table entries (the reference fixes 1e8, dsgl.hpp:82) */
   uint64_t seed;       /* stochastic-rounding stream seed                         */
+  int32_t forward_tile;/* persistent engine, lanes per input row in the forward dot
+                          products: 1 = one lane per input; 2 = two lanes per input while
+                          at most 16 inputs remain (d <= 128, K <= 5 only; the same sums);
+                          0 = chosen by the autotuner                              */
+  int32_t reserved;    /* 0                                                       */
 } sgns_options;
 
 typedef struct sgns_stats {
@@ -97,6 +102,9 @@ typedef struct sgns_stats {
   uint64_t row_loads;          /* table rows copied into worker buffers              */
   uint64_t row_stores;         /* table rows written back from worker buffers        */
   uint64_t output_rows;        /* sum over steps of the output rows (targets + negatives) */
+  int32_t forward_tile;        /* persistent engine: lanes per input in the forward      */
+  int32_t warps_per_worker;    /* warps that train one worker (one: its state lives in
+                                  that warp's registers and shared memory)              */
 } sgns_stats;
 
 /* Defaults of dsgl.hpp:67-76, table_size 1e8, persistent engine, fp32. */

@@ -65,12 +65,13 @@ def case(name):
     return cfg, corpus.astype(np.int32), None
 
 
-def gpu_train(cfg, corpus, engine, storage, workers=1, wpc=1, table_size=None, table_threads=2, mode="hogwild"):
+def gpu_train(cfg, corpus, engine, storage, workers=1, wpc=1, table_size=None, table_threads=2, mode="hogwild",
+              tile=0):
     counts = np.bincount(corpus[corpus >= 0], minlength=cfg["V"]).astype(np.int32)
     opt = sgns.default_options(size=cfg["d"], window=cfg["window"], negative=cfg["negative"], iter=cfg["iter"],
                                sample=cfg["sample"], alpha=cfg["alpha"], engine=engine, storage=storage,
                                workers=workers, warps_per_cta=wpc, threads=table_threads,
-                               table_size=table_size or 1000000, debug=0, mode=mode)
+                               table_size=table_size or 1000000, debug=0, mode=mode, forward_tile=tile)
     with sgns.Trainer(opt) as t:
         t.set_vocab(counts)
         st = t.train_corpus(corpus)
@@ -165,6 +166,20 @@ def test_persistent_matches_oracle(name, storage, wpc, sgns_lib, oracle_mod):
     assert abs(st.final_alpha - ost["final_alpha"]) == 0
     assert np.array_equal(wih.view(np.uint32), owih.view(np.uint32)), np.abs(wih - owih).max()
     assert np.array_equal(woh.view(np.uint32), owoh.view(np.uint32)), np.abs(woh - owoh).max()
+
+
+@pytest.mark.parametrize("tile", [1, 2])
+@pytest.mark.parametrize("storage", ["fp32", "bf16"])
+@pytest.mark.parametrize("name", ["cl_d128", "basic"])
+def test_forward_tiles_match_oracle(name, storage, tile, sgns_lib, oracle_mod):
+    """Both forward tiles (one or two lanes per input) compute the window policy's sums in
+    the same order: bit for bit the oracle, one worker."""
+    cfg, corpus, _ = case(name)
+    wih, woh, st, _ = gpu_train(cfg, corpus, "persistent", storage, tile=tile)
+    owih, owoh, _ = oracle_train(oracle_mod, cfg, corpus, oracle_mod.POLICY_WINDOW, storage)
+    assert st.forward_tile == tile and st.warps_per_worker == 1
+    assert np.array_equal(wih.view(np.uint32), owih.view(np.uint32))
+    assert np.array_equal(woh.view(np.uint32), owoh.view(np.uint32))
 
 
 @pytest.mark.parametrize("engine,storage", [("plain", "fp32"), ("persistent", "fp32"), ("persistent", "bf16")])
@@ -268,14 +283,15 @@ def test_autotuner_cache_file(sgns_lib, tmp_path, monkeypatch):
         with sgns.Trainer(size=cfg["d"], window=cfg["window"], negative=cfg["negative"], table_size=1000000,
                           debug=0, storage="bf16") as t:
             t.set_vocab(counts)
-            return t.train_corpus(corpus).warps_per_cta
+            st = t.train_corpus(corpus)
+            return st.warps_per_cta, st.forward_tile
 
-    first = run()
+    first, tile = run()
     lines = cache.read_text().splitlines()
-    assert len(lines) == 1 and lines[0].endswith("\t%d" % first)
+    assert len(lines) == 1 and lines[0].endswith("\t%d\t%d" % (first, tile)) and tile in (1, 2)
     planted = 3 if first != 3 else 2  # the last entry of a key wins
-    cache.write_text(lines[0].rsplit("\t", 1)[0] + "\t%d\n" % planted, encoding="utf-8")
-    assert run() == planted
+    cache.write_text(lines[0].split("\t")[0] + "\t%d\t%d\n" % (planted, 3 - tile), encoding="utf-8")
+    assert run() == (planted, 3 - tile)
 
 
 @pytest.mark.parametrize("engine,policy", [("plain", 0), ("persistent", 1)])
