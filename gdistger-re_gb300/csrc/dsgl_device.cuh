@@ -205,8 +205,10 @@ __device__ __forceinline__ NegDraw neg_draw_issue(const TrainParams& p, const Sm
 // the outputs t1, negatives, t2; they are stored t1, t2, negatives, so that target 2 sits
 // at a fixed index (a run-time index into register arrays would put them in local
 // memory).  Every sum whose order matters walks them in the reference's order.
+// t2_meta: multiplicity of target 2 (0 in single-window steps, where t2 is a placeholder
+// whose coefficients are zero and whose row is not written)
 __device__ __forceinline__ int select_outputs(const TrainParams& p, NegDraw nd, int t1, int t2, int* out_id,
-                                              int* out_meta) {
+                                              int* out_meta, int t2_meta = 1) {
   const int lane = lane_id();
   const bool valid = lane < p.K;
   int s = -2 - lane;
@@ -224,7 +226,7 @@ __device__ __forceinline__ int select_outputs(const TrainParams& p, NegDraw nd, 
     out_id[0] = t1;
     out_meta[0] = 1;
     out_id[1] = t2;
-    out_meta[1] = 1;
+    out_meta[1] = t2_meta;
   }
   __syncwarp();
   return O;
@@ -233,7 +235,7 @@ __device__ __forceinline__ int select_outputs(const TrainParams& p, NegDraw nd, 
 // Same output list from K stored draws words[0..K) (the reference's neg_words group);
 // also returns, for each output i in 1..O-2, the index k of its first draw in kidx.
 __device__ __forceinline__ int select_outputs_stored(int K, const int* words, int t1, int t2,
-                                                     int* out_id, int* out_meta, int* kidx) {
+                                                     int* out_id, int* out_meta, int* kidx, int t2_meta = 1) {
   const int lane = lane_id();
   const bool valid = lane < K;
   const int s = valid ? words[lane] : -2 - lane;
@@ -251,7 +253,7 @@ __device__ __forceinline__ int select_outputs_stored(int K, const int* words, in
     out_id[0] = t1;
     out_meta[0] = 1;
     out_id[O - 1] = t2;
-    out_meta[O - 1] = 1;
+    out_meta[O - 1] = t2_meta;
   }
   __syncwarp();
   return O;

@@ -159,6 +159,10 @@ __global__ void __launch_bounds__(32 * kPlainWarps) plain_step_kernel(TrainParam
   float* negbuf = reinterpret_cast<float*>(scr + L.negbuf);
   int len[2] = {st.len0, st.len1}, pos[2] = {st.pos0, st.pos1}, nu[2] = {st.nu0, st.nu1};
   float loss = 0.f;
+  // windows per step: two walks (the reference's step) or one; a single-window step keeps
+  // target 2's slot as a placeholder copy of target 1 with multiplicity 0
+  const bool two = p.windows == 2;
+  const int n_walks = two ? 2 : 1;
 
   do {
     if (st.word_count - st.last_wc > 10000) {  // dsgl.hpp:886-897
@@ -170,7 +174,7 @@ __global__ void __launch_bounds__(32 * kPlainWarps) plain_step_kernel(TrainParam
       st.last_wc = st.word_count;
       __syncwarp();
     }
-    for (int walk = 0; walk < 2; walk++) {  // dsgl.hpp:902-1030
+    for (int walk = 0; walk < n_walks; walk++) {  // dsgl.hpp:902-1030
       while (len[walk] == 0) {
         if (st.cur >= st.end) break;
         int* wsen = sen + walk * lmax;
@@ -209,7 +213,7 @@ __global__ void __launch_bounds__(32 * kPlainWarps) plain_step_kernel(TrainParam
     }
     if (st.change_neg) {  // dsgl.hpp:1054-1088
       const uint64_t base = st.rng;
-      st.neg_n = len[0] > len[1] ? len[0] : len[1];
+      st.neg_n = two && len[1] > len[0] ? len[1] : len[0];
       const int total = st.neg_n * K;
       uint64_t chunk = base;
       for (int c0 = 0; c0 < total; c0 += 32) {
@@ -233,16 +237,17 @@ __global__ void __launch_bounds__(32 * kPlainWarps) plain_step_kernel(TrainParam
     }
 
     // ---- one step (dsgl.hpp:1089-1368) ----
-    const int t1 = sen[pos[0]], t2 = sen[lmax + pos[1]];
+    const int t1 = sen[pos[0]], t2 = two ? sen[lmax + pos[1]] : t1;
     st.rng = lcg_next(st.rng);
     const int b = (int)fast_mod(st.rng, p.div_window);
     const int I0 = window_inputs(pos[0], len[0], w, b, 0, in_off,
                                  [&](int c) { return slot[c]; });
-    const int I = I0 + window_inputs(pos[1], len[1], w, b, I0, in_off,
-                                     [&](int c) { return lmax + slot[lmax + c]; });
+    const int I = I0 + (two ? window_inputs(pos[1], len[1], w, b, I0, in_off,
+                                            [&](int c) { return lmax + slot[lmax + c]; })
+                            : 0);
     st.neg_count++;
     const int g = st.neg_count % st.neg_n;
-    const int O = select_outputs_stored(K, negw + (size_t)g * K, t1, t2, out_id, out_meta, kidx);
+    const int O = select_outputs_stored(K, negw + (size_t)g * K, t1, t2, out_id, out_meta, kidx, two ? 1 : 0);
     {  // outputs: targets from Woh (global), negatives from the pool buffer
       float4 v[kOMax][DCH];
       const int d4 = d >> 2;
@@ -284,7 +289,7 @@ __global__ void __launch_bounds__(32 * kPlainWarps) plain_step_kernel(TrainParam
             if (i == O - 1) mlast = md[i][t];
           // Woh[target] += outputMd, re-reading the table as the reference does
           RowIO<S>::store4(p.woh, t1, d, q, add4(RowIO<S>::load4(p.woh, t1, d, q), md[0][t]), e1);
-          RowIO<S>::store4(p.woh, t2, d, q, add4(RowIO<S>::load4(p.woh, t2, d, q), mlast), e2);
+          if (two) RowIO<S>::store4(p.woh, t2, d, q, add4(RowIO<S>::load4(p.woh, t2, d, q), mlast), e2);
 #pragma unroll
           for (int i = 1; i < kOMax - 1; i++) {
             if (i < O - 1) {
@@ -296,13 +301,13 @@ __global__ void __launch_bounds__(32 * kPlainWarps) plain_step_kernel(TrainParam
       }
     }
     st.pairs += (unsigned long long)I;
-    st.outs += (unsigned long long)O;
+    st.outs += (unsigned long long)(two ? O : O - 1);
     st.steps++;
     __syncwarp();
 
     pos[0]++;
     pos[1]++;
-    for (int walk = 0; walk < 2; walk++) {  // dsgl.hpp:1377-1398
+    for (int walk = 0; walk < n_walks; walk++) {  // dsgl.hpp:1377-1398
       if (pos[walk] >= len[walk]) {
         const uint64_t ev =
             S == STORE_BF16 ? sr_event_key(p.sr_seed, EV_WALK0 + walk, (uint32_t)wid, st.step_id) : 0;

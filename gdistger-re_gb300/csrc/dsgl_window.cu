@@ -119,8 +119,9 @@ __device__ __forceinline__ void store_row_from_smem(void* tab, int64_t row, int 
 // d known, every shared-memory address of the step is a base register plus an immediate
 // offset and the column-range guards vanish; the arithmetic is the same either way.
 // TILE: lanes per input in the forward dot products (2: two lanes share an input while at
-// most 16 inputs remain; the same bits), chosen by the autotuner.
-template <int S, int DCH, int OM, bool kLoss, int DFIX, int TILE>
+// most 16 inputs remain; the same bits), chosen by the autotuner.  NW: windows per step (2,
+// the reference's step over two walks; 1, one walk per step).
+template <int S, int DCH, int OM, bool kLoss, int DFIX, int TILE, int NW = 2>
 __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
   extern __shared__ __align__(16) float smem[];
   float* exp_s = smem;
@@ -137,6 +138,11 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
   if (wid >= p.workers) return;
 
   const int d = DFIX ? DFIX : p.d, w = p.window, K = p.K;
+  // windows per step: two walks (the reference's step) or one; a single-window step keeps
+  // target 2's slot as a placeholder copy of target 1 with multiplicity 0 (no coefficient,
+  // no write)
+  constexpr bool two = NW == 2;
+  constexpr int n_walks = NW;
   const WinLayout L = win_layout(d, w, K, p.lmax);
   float* base = smem + kHdrWords + (threadIdx.x >> 5) * L.words;
   float* rows = base + L.rows;
@@ -274,8 +280,8 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     }
     // Rare paths (learning-rate update, walk refill, epoch end, pool change, walk end) are
     // marked unlikely so the compiler keeps them off the per-step instruction stream.
-    if (__builtin_expect(len[0] == 0 || len[1] == 0, 0))
-    for (int walk = 0; walk < 2; walk++) {  // dsgl.hpp:902-1030
+    if (__builtin_expect(len[0] == 0 || (two && len[1] == 0), 0))
+    for (int walk = 0; walk < n_walks; walk++) {  // dsgl.hpp:902-1030
       while (len[walk] == 0) {
         if (cur >= end) break;
         const int n = fill_walk(p, *sj, sen + walk * lmax, cur, end, word_count, rng, lmax);
@@ -299,7 +305,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     }
     if (__builtin_expect(change_neg, 0)) {  // dsgl.hpp:1054-1088: the pool is its base state and size
       pool_base = rng;
-      neg_n = len[0] > len[1] ? len[0] : len[1];
+      neg_n = two && len[1] > len[0] ? len[1] : len[0];
       neg_g = neg_count % neg_n;
       rng = jump_any(rng, (uint64_t)neg_n * (uint64_t)K, p.jumps);
       change_neg = false;
@@ -313,7 +319,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     // holds the key of event kind k (targets 1 and 2, walks 0 and 1, negatives).
     const uint64_t sr_key =
         S == STORE_BF16 && lane <= EV_NEG ? sr_event_key(p.sr_seed, lane, (uint32_t)wid, step_id) : 0;
-    const int t1 = sen[pos[0]], t2 = sen[lmax + pos[1]];
+    const int t1 = sen[pos[0]], t2 = two ? sen[lmax + pos[1]] : t1;
     neg_count++;
     neg_g = neg_g + 1 == neg_n ? 0 : neg_g + 1;
     const int g = neg_g;
@@ -332,12 +338,12 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     grp_g = g;
     const int d4 = d >> 2;
     // a walk that ends at this step completes at its transition below
-    const bool end0 = pos[0] + 1 >= len[0], end1 = pos[1] + 1 >= len[1];
+    const bool end0 = pos[0] + 1 >= len[0], end1 = two && pos[1] + 1 >= len[1];
     int O;
     if (kPrefetchRows && __builtin_expect(ov_ready, 1)) {
       O = O_next;  // select_outputs and the gather ran at the end of the previous step
     } else {
-      O = select_outputs(p, nd, t1, t2, out_id, out_meta);
+      O = select_outputs(p, nd, t1, t2, out_id, out_meta, two ? 1 : 0);
       // Gather the output rows (targets and negatives) from Woh: every load is issued here
       // and kept raw; the window input lists are built while they are in flight.
 #pragma unroll
@@ -368,8 +374,9 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     const int b = (int)fast_mod(rng, p.div_window);
     const int I0 = window_inputs<true>(pos[0], len[0], w, b, 0, in_row,
                                  [&](int c) { return __shfl_sync(kFull, rg0, c & (kRing - 1)); });
-    const int I = I0 + window_inputs<true>(pos[1], len[1], w, b, I0, in_row,
-                                     [&](int c) { return NS + __shfl_sync(kFull, rg1, c & (kRing - 1)); });
+    const int I = I0 + (two ? window_inputs<true>(pos[1], len[1], w, b, I0, in_row,
+                                                [&](int c) { return NS + __shfl_sync(kFull, rg1, c & (kRing - 1)); })
+                            : 0);
 #pragma unroll
     for (int i = 0; i < OM; i++)
 #pragma unroll
@@ -421,8 +428,11 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
           // outputs are stored t1, t2, negatives (see select_outputs)
           const float4 b1 = reinterpret_cast<const float4*>(out_rows)[q];
           const float4 n1 = RowIO<S>::store4(p.woh, t1, d, q, add4(b1, md[0][t]), e1);
-          const float4 b2 = t2 == t1 ? n1 : reinterpret_cast<const float4*>(out_rows + DP)[q];
-          const float4 n2 = RowIO<S>::store4(p.woh, t2, d, q, add4(b2, md[1][t]), e2);
+          float4 n2 = n1;
+          if (two) {
+            const float4 b2 = t2 == t1 ? n1 : reinterpret_cast<const float4*>(out_rows + DP)[q];
+            n2 = RowIO<S>::store4(p.woh, t2, d, q, add4(b2, md[1][t]), e2);
+          }
 #pragma unroll
           for (int i = 2; i < OM; i++) {
             if (i < O) {
@@ -435,7 +445,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
       }
     }
     n_pairs += (unsigned long long)I;
-    n_outs += (unsigned long long)O;
+    n_outs += (unsigned long long)(two ? O : O - 1);
     n_steps++;
     __syncwarp();
     // Both walks go on and the pool stays: select the next step's outputs and issue their
@@ -443,8 +453,8 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
     // updated rows); the window transitions below run while they are in flight.
     ov_ready = false;
     if (kPrefetchRows && !end0 && !end1 && pf_g >= 0) {
-      const int t1n = sen[pos[0] + 1], t2n = sen[lmax + pos[1] + 1];
-      O_next = select_outputs(p, pf, t1n, t2n, out_id, out_meta);
+      const int t1n = sen[pos[0] + 1], t2n = two ? sen[lmax + pos[1] + 1] : t1n;
+      O_next = select_outputs(p, pf, t1n, t2n, out_id, out_meta, two ? 1 : 0);
 #pragma unroll
       for (int i = 0; i < OM; i++) {
         const int row = i < O_next ? out_id[i] : 0;
@@ -467,7 +477,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
       // set-up.  A later write-back of the same vertex in this transition (walk 0's leave
       // or flush before walk 1's enter reads) is ordered after the load by program order.
       const int d4 = d >> 2;
-      for (int walk = 0; walk < 2; walk++) {
+      for (int walk = 0; walk < n_walks; walk++) {
         const uint64_t ev = S == STORE_BF16 ? __shfl_sync(kFull, sr_key, EV_WALK0 + walk) : 0;
         if (__builtin_expect(pos[walk] >= len[walk], 0)) {
           flush_walk(walk, ev);
@@ -557,14 +567,14 @@ static cudaError_t occupancy_t(int d, int w, int K, int lmax, int wpc, int tile,
   return occupancy_tile<S, DCH, OM, 0>(d, w, K, lmax, wpc, tile, ctas);
 }
 
-template <int S, int DCH, int OM, bool kLoss, int DFIX, int TILE>
+template <int S, int DCH, int OM, bool kLoss, int DFIX, int TILE, int NW = 2>
 static cudaError_t launch_loss_t(const TrainParams& p, int wpc, cudaStream_t s) {
   const size_t smem = window_smem_bytes(p.d, p.window, p.K, p.lmax, wpc);
-  cudaError_t e = cudaFuncSetAttribute(window_engine_kernel<S, DCH, OM, kLoss, DFIX, TILE>,
+  cudaError_t e = cudaFuncSetAttribute(window_engine_kernel<S, DCH, OM, kLoss, DFIX, TILE, NW>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const int blocks = (p.workers + wpc - 1) / wpc;
-  window_engine_kernel<S, DCH, OM, kLoss, DFIX, TILE><<<blocks, 32 * wpc, smem, s>>>(p);
+  window_engine_kernel<S, DCH, OM, kLoss, DFIX, TILE, NW><<<blocks, 32 * wpc, smem, s>>>(p);
   return cudaGetLastError();
 }
 template <int S, int DCH, int OM, bool kLoss, int DFIX>
@@ -575,6 +585,10 @@ static cudaError_t launch_tile_t(const TrainParams& p, int wpc, cudaStream_t s) 
 }
 template <int S, int DCH, int OM>
 static cudaError_t launch_t(const TrainParams& p, int wpc, cudaStream_t s) {
+  // single-window steps: the generic kernel (run-time d, one lane per input)
+  if (p.windows == 1)
+    return p.compute_loss ? launch_loss_t<S, DCH, OM, true, 0, 1, 1>(p, wpc, s)
+                          : launch_loss_t<S, DCH, OM, false, 0, 1, 1>(p, wpc, s);
   if (p.compute_loss) return launch_tile_t<S, DCH, OM, true, 0>(p, wpc, s);
   const int f = fixed_d(p.d);
   if constexpr (DCH == 1) {

@@ -298,6 +298,8 @@ sgns_status validate(sgns_handle* h, const sgns_options& o) {
     return fail(h, SGNS_EINVAL, "workers/warps_per_cta out of range");
   if (o.mode != SGNS_MODE_HOGWILD && o.mode != SGNS_MODE_REPLAY_EXACT)
     return fail(h, SGNS_EINVAL, "unknown mode %d", o.mode);
+  if (o.windows_per_step < 0 || o.windows_per_step > 2)
+    return fail(h, SGNS_EINVAL, "windows_per_step %d: 1 or 2 (0 = 2)", o.windows_per_step);
   if (o.forward_tile < 0 || o.forward_tile > 2)
     return fail(h, SGNS_EINVAL, "forward_tile %d: 0 (tuned), 1 or 2", o.forward_tile);
   if (o.forward_tile == 2 && !window_engine_has_tile2(o.size, o.negative))
@@ -335,6 +337,7 @@ TrainParams make_params(sgns_handle* h, int workers) {
   p.lmax = h->lmax;
   p.storage = o.storage == SGNS_STORE_BF16_SR ? STORE_BF16 : STORE_F32;
   p.fwd_tile = h->tile;
+  p.windows = o.windows_per_step == 1 ? 1 : 2;
   p.ctr = h->d_ctr;
   return p;
 }
@@ -364,7 +367,8 @@ sgns_status finish_stats(sgns_handle* h, int workers, float ms) {
   s.train_ms = ms;
   s.workers = workers;
   s.warps_per_cta = h->opt.engine == SGNS_ENGINE_PERSISTENT ? h->wpc : 4;
-  s.forward_tile = h->opt.engine == SGNS_ENGINE_PERSISTENT ? h->tile : 0;
+  // single-window steps run the one-lane kernel
+  s.forward_tile = h->opt.engine != SGNS_ENGINE_PERSISTENT ? 0 : h->opt.windows_per_step == 1 ? 1 : h->tile;
   s.warps_per_worker = 1;
   s.row_loads = c.row_loads;
   s.row_stores = c.row_stores;
@@ -763,6 +767,7 @@ void sgns_default_options(sgns_options* o) {
   o->engine = SGNS_ENGINE_PERSISTENT;
   o->table_size = 100000000;  // dsgl.hpp:82
   o->seed = 0x5EEDULL;
+  o->windows_per_step = 2;
 }
 
 sgns_status sgns_options_from_args(sgns_options* o, int argc, const char* const* argv) {
@@ -778,7 +783,8 @@ sgns_status sgns_options_from_args(sgns_options* o, int argc, const char* const*
               {"-window", &o->window},     {"-negative", &o->negative},   {"-threads", &o->threads},
               {"-iter", &o->iter},         {"-min-count", &o->min_count}, {"-batch-size", &o->batch_size},
               {"-workers", &o->workers},   {"-warps-per-cta", &o->warps_per_cta},
-              {"-forward-tile", &o->forward_tile}, {"-device", &o->device},
+              {"-forward-tile", &o->forward_tile}, {"-windows-per-step", &o->windows_per_step},
+              {"-device", &o->device},
               {"-loss", &o->compute_loss}};
   for (auto& f : ints) {
     int i = pos(f.name);

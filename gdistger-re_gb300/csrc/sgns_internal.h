@@ -149,6 +149,8 @@ struct TrainParams {
   uint64_t sr_seed;
   int32_t compute_loss, lmax, storage;
   int32_t fwd_tile;                // lanes per input in the forward (1, or 2 where supported)
+  int32_t windows;                 // windows per step: 2 (two walks, dsgl.hpp:1100-1132) or 1
+  int32_t pad2;
   DeviceCounters* ctr;
   // plain-engine state (HBM)
   void* plain_state;

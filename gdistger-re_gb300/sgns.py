@@ -29,7 +29,7 @@ class Options(ctypes.Structure):
         ("engine", ctypes.c_int32), ("workers", ctypes.c_int32), ("warps_per_cta", ctypes.c_int32),
         ("device", ctypes.c_int32), ("compute_loss", ctypes.c_int32), ("mode", ctypes.c_int32),
         ("table_size", ctypes.c_int64), ("seed", ctypes.c_uint64), ("forward_tile", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("windows_per_step", ctypes.c_int32),
     ]
 
 

@@ -84,7 +84,10 @@ typedef struct sgns_options {
                           products: 1 = one lane per input; 2 = two lanes per input while
                           at most 16 inputs remain (d <= 128, K <= 5 only; the same sums);
                           0 = chosen by the autotuner                              */
-  int32_t reserved;    /* 0                                                       */
+  int32_t windows_per_step; /* 2 (or 0): the reference's step over two walks, target 1
+                          labelling walk 1's window and target 2 walk 2's (dsgl.hpp:
+                          1100-1159); 1: one walk per step -- its window and target with
+                          the shared negatives (-windows-per-step 1)               */
 } sgns_options;
 
 typedef struct sgns_stats {

@@ -192,6 +192,8 @@ struct Shared {
   int64_t V;
   const float* exp_table;
   int d, window, negative, iter, workers, policy;
+  int windows;  // 2: two walks per step (dsgl.hpp:1100-1132); 1: one walk, target 2 a
+                // placeholder copy of target 1 with multiplicity 0, never written
   float sample, start_alpha;
   uint64_t train_words;
   uint64_t sr_seed;
@@ -377,7 +379,7 @@ struct Worker {
   void build_pool() {
     neg_words.clear();
     neg_buffer.clear();
-    neg_batch_num = std::max(len[0], len[1]);
+    neg_batch_num = sh.windows == 2 ? std::max(len[0], len[1]) : len[0];
     for (int i = 0; i < neg_batch_num; i++) {
       for (int k = 0; k < K; k++) {
         rng = lcg_next(rng);
@@ -407,11 +409,12 @@ struct Worker {
   void step() {
     const int w = window;
     const uint64_t ev_step = step_id;
-    const int t1 = sen[0][pos[0]], t2 = sen[1][pos[1]];
+    const bool two = sh.windows == 2;
+    const int t1 = sen[0][pos[0]], t2 = two ? sen[1][pos[1]] : t1;
     rng = lcg_next(rng);
     const int b = (int)(rng % (uint64_t)w);
     int I = 0, first = 0;
-    for (int walk = 0; walk < 2; walk++) {
+    for (int walk = 0; walk < (two ? 2 : 1); walk++) {
       for (int i = b; i < 2 * w + 1 - b; i++) {
         if (i == w) continue;
         int c = pos[walk] - w + i;
@@ -444,7 +447,7 @@ struct Worker {
     out_id[0] = t1;
     out_meta[0] = 1;
     out_id[off] = t2;
-    out_meta[off] = 1;
+    out_meta[off] = two ? 1 : 0;
     const int O = off + 1;
 
     // gather (dsgl.hpp:1173-1211)
@@ -526,7 +529,7 @@ struct Worker {
       const A* m2 = &outputMd[(size_t)(O - 1) * d];
       for (int c = 0; c < d; c++) {
         ST::store(r1 + c, ST::load(r1 + c) + m1[c], e1, (uint32_t)t1, c);
-        ST::store(r2 + c, ST::load(r2 + c) + m2[c], e2, (uint32_t)t2, c);
+        if (two) ST::store(r2 + c, ST::load(r2 + c) + m2[c], e2, (uint32_t)t2, c);
       }
     }
     if (sh.policy == POLICY_REF) {
@@ -548,7 +551,7 @@ struct Worker {
     // positions, flushes (dsgl.hpp:1372-1407)
     pos[0]++;
     pos[1]++;
-    for (int walk = 0; walk < 2; walk++) {
+    for (int walk = 0; walk < (two ? 2 : 1); walk++) {
       uint64_t ev = sr_event_key(sh.sr_seed, EV_WALK0 + walk, wid, ev_step);
       if (pos[walk] >= len[walk]) {
         if (sh.policy == POLICY_REF) ref_flush_walk(walk);
@@ -584,7 +587,7 @@ struct Worker {
       if (a < sh.start_alpha * 0.0001f) a = sh.start_alpha * 0.0001f;
       sh.alpha.store(a, std::memory_order_relaxed);
     }
-    for (int w = 0; w < 2; w++) {
+    for (int w = 0; w < sh.windows; w++) {
       while (len[w] == 0) {
         if (slice_done()) break;
         fill_walk(w);
@@ -671,6 +674,8 @@ struct oracle_config {
   int64_t table_size;
   float sample, alpha;
   uint64_t sr_seed;
+  int32_t windows;        // windows per step: 2 (the reference's two walks) or 1
+  int32_t pad_;
 };
 
 struct oracle_stats {
@@ -735,6 +740,7 @@ int oracle_train(const oracle_config* cfg, const int32_t* counts, int64_t V, con
   sh.iter = cfg->iter;
   sh.workers = cfg->workers;
   sh.policy = cfg->policy;
+  sh.windows = cfg->windows == 1 ? 1 : 2;
   sh.sample = cfg->sample;
   sh.start_alpha = cfg->alpha;
   sh.train_words = train_words;

@@ -21,7 +21,8 @@ class Config(ctypes.Structure):
                 ("iter", ctypes.c_int32), ("workers", ctypes.c_int32), ("threads", ctypes.c_int32),
                 ("table_threads", ctypes.c_int32), ("policy", ctypes.c_int32), ("storage", ctypes.c_int32),
                 ("schedule", ctypes.c_int32), ("table_size", ctypes.c_int64), ("sample", ctypes.c_float),
-                ("alpha", ctypes.c_float), ("sr_seed", ctypes.c_uint64)]
+                ("alpha", ctypes.c_float), ("sr_seed", ctypes.c_uint64), ("windows", ctypes.c_int32),
+                ("pad_", ctypes.c_int32)]
 
 
 class Stats(ctypes.Structure):
@@ -148,7 +149,7 @@ def init_wih(V, d):
 
 def train(corpus, counts, d=16, window=5, negative=5, iter=1, workers=1, threads=1, table_threads=12,
           policy=POLICY_REF, storage=STORE_F32, table_size=100000000, sample=1e-3, alpha=0.025,
-          sr_seed=0x5EED, schedule=0):
+          sr_seed=0x5EED, schedule=0, windows=2):
     """Runs the restated trainer; returns (Wih, Woh, stats) in sorted-row order.
 
     Wih starts from the reference initialisation (bf16: rounded to nearest even),
@@ -168,7 +169,7 @@ def train(corpus, counts, d=16, window=5, negative=5, iter=1, workers=1, threads
         wih, woh = w0.astype(np.float64), np.zeros((V, d), np.float64)
     cfg = Config(d=d, window=window, negative=negative, iter=iter, workers=workers, threads=threads,
                  table_threads=table_threads, policy=policy, storage=storage, table_size=table_size,
-                 sample=sample, alpha=alpha, sr_seed=sr_seed, schedule=schedule)
+                 sample=sample, alpha=alpha, sr_seed=sr_seed, schedule=schedule, windows=windows)
     st = Stats()
     rc = lib().oracle_train(ctypes.byref(cfg), _p(counts), V, _p(corpus), len(corpus), _p(wih), _p(woh),
                             ctypes.byref(st))

@@ -66,25 +66,26 @@ def case(name):
 
 
 def gpu_train(cfg, corpus, engine, storage, workers=1, wpc=1, table_size=None, table_threads=2, mode="hogwild",
-              tile=0):
+              tile=0, windows=2):
     counts = np.bincount(corpus[corpus >= 0], minlength=cfg["V"]).astype(np.int32)
     opt = sgns.default_options(size=cfg["d"], window=cfg["window"], negative=cfg["negative"], iter=cfg["iter"],
                                sample=cfg["sample"], alpha=cfg["alpha"], engine=engine, storage=storage,
                                workers=workers, warps_per_cta=wpc, threads=table_threads,
-                               table_size=table_size or 1000000, debug=0, mode=mode, forward_tile=tile)
+                               table_size=table_size or 1000000, debug=0, mode=mode, forward_tile=tile,
+                               windows_per_step=windows)
     with sgns.Trainer(opt) as t:
         t.set_vocab(counts)
         st = t.train_corpus(corpus)
         return t.embeddings(0), t.embeddings(1), st, t.order()
 
 
-def oracle_train(oracle_mod, cfg, corpus, policy, storage, workers=1, table_size=None, table_threads=2):
+def oracle_train(oracle_mod, cfg, corpus, policy, storage, workers=1, table_size=None, table_threads=2, windows=2):
     counts = np.bincount(corpus[corpus >= 0], minlength=cfg["V"]).astype(np.int32)
     st = {"fp32": oracle_mod.STORE_F32, "bf16": oracle_mod.STORE_BF16}[storage]
     wih, woh, stats = oracle_mod.train(corpus, counts, d=cfg["d"], window=cfg["window"], negative=cfg["negative"],
                                        iter=cfg["iter"], workers=workers, threads=1, table_threads=table_threads,
                                        policy=policy, storage=st, table_size=table_size or 1000000,
-                                       sample=cfg["sample"], alpha=cfg["alpha"])
+                                       sample=cfg["sample"], alpha=cfg["alpha"], windows=windows)
     if storage == "bf16":
         wih, woh = oracle_mod.bf16_to_f32(wih), oracle_mod.bf16_to_f32(woh)
     return wih, woh, stats
@@ -166,6 +167,23 @@ def test_persistent_matches_oracle(name, storage, wpc, sgns_lib, oracle_mod):
     assert abs(st.final_alpha - ost["final_alpha"]) == 0
     assert np.array_equal(wih.view(np.uint32), owih.view(np.uint32)), np.abs(wih - owih).max()
     assert np.array_equal(woh.view(np.uint32), owoh.view(np.uint32)), np.abs(woh - owoh).max()
+
+
+@pytest.mark.parametrize("engine,storage", [("plain", "fp32"), ("persistent", "fp32"), ("persistent", "bf16")])
+@pytest.mark.parametrize("name", ["cl_d128", "basic", "sbm_d64_w15"])
+def test_single_window_steps_match_oracle(name, engine, storage, sgns_lib, oracle_mod):
+    """windows_per_step = 1: one walk per step, its window and target with the shared
+    negatives; bit for bit the oracle's statement of the same step, one worker."""
+    cfg, corpus, _ = case(name)
+    wih, woh, st, _ = gpu_train(cfg, corpus, engine, storage, windows=1)
+    policy = oracle_mod.POLICY_REF if engine == "plain" else oracle_mod.POLICY_WINDOW
+    owih, owoh, ost = oracle_train(oracle_mod, cfg, corpus, policy, storage, windows=1)
+    assert (st.steps, st.pairs, st.word_count_actual) == (ost["steps"], ost["pairs"], ost["word_count_actual"])
+    assert np.array_equal(wih.view(np.uint32), owih.view(np.uint32))
+    assert np.array_equal(woh.view(np.uint32), owoh.view(np.uint32))
+    # one window per step: about half the pairs of a two-window step
+    _, _, st2, _ = gpu_train(cfg, corpus, engine, storage)
+    assert st.steps > 1.5 * st2.steps and st.pairs < 0.8 * st2.pairs * st.steps / st2.steps
 
 
 @pytest.mark.parametrize("tile", [1, 2])

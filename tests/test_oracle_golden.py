@@ -131,3 +131,17 @@ def test_round_robin_schedule_keeps_the_control_flow(policy, oracle_mod):
                                     sample=meta["sample"], alpha=meta["alpha"], schedule=schedule)
         runs.append((st["steps"], st["pairs"], st["word_count_actual"]))
     assert runs[0][0] > 0 and runs[0] == runs[1] == runs[2], runs
+
+
+def test_single_window_step_count(oracle_mod):
+    """windows_per_step = 1 without subsampling: one step per position of every walk of
+    length > 1 except the pass's last walk, which the reference discards unflushed when the
+    slice ends (dsgl.hpp:1031-1050)."""
+    rng = np.random.default_rng(4)
+    walks = [rng.integers(0, 1200, rng.integers(1, 40)).tolist() for _ in range(300)]
+    corpus = np.array([t for w in walks for t in w + [-1]], np.int32)
+    counts = np.bincount(corpus[corpus >= 0], minlength=1200).astype(np.int32)
+    _, _, st = oracle_mod.train(corpus, counts, d=8, window=3, negative=4, iter=1, workers=1, threads=1,
+                                table_threads=2, table_size=100000, sample=0.0, windows=1)
+    kept = [len(w) for w in walks if len(w) > 1]
+    assert st["steps"] == sum(kept[:-1])
