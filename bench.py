@@ -503,6 +503,43 @@ def run_minibatch_error(args):
     print(json.dumps({"mode": "minibatch-error", "workload": args.workload, **res}), flush=True)
 
 
+def run_walks(args):
+    """--walks: the information-oriented walk generator alone (configuration 2's corpus
+    producer): SBM with V vertices (4 blocks, p_in/p_out 20, 2.73 edges per vertex), 10%
+    holdout, 10 walkers per vertex, min length 20, cap 80; with and without trace steps.
+    Common-neighbour counts and walks on the GPU; tokens per second and the gather rate."""
+    import torch
+    import sgns
+    import synth
+
+    V = args.walk_vertices
+    ip, ix, _ = synth.sbm_csr(V, int(2.73 * V), 4, 20.0, seed=1)
+    tip, tix, _, _ = synth.holdout_csr(ip, ix, 0.1, seed=1001)
+    dip, dix = torch.from_numpy(tip).cuda(), torch.from_numpy(tix).cuda()
+    dcn = torch.empty(len(tix), dtype=torch.int32, device="cuda")
+    out = {"mode": "walks", "graph": "SBM V=%d E=%d (training edges)" % (V, len(tix) // 2), "walkers": 10 * V}
+    for rep in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sgns.edge_common_neighbors(dip, dix, dcn)
+        torch.cuda.synchronize()
+        out["common_neighbors_ms"] = 1e3 * (time.perf_counter() - t0)
+    for trace, r_th in ((0, 0.84), (1, 0.78)):
+        best = None
+        for rep in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            corpus, n_tok = sgns.info_walks(dip, dix, dcn, 10 * V, 20, 80, r_th, 2001, trace=trace)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+            del corpus
+        moves = n_tok - 2 * 10 * V
+        out["trace_%d" % trace] = {"r_threshold": r_th, "tokens": int(n_tok), "ms": 1e3 * best,
+                                   "tokens_per_s": n_tok / best, "walk_gather_GBs": 2 * 40.0 * moves / best / 1e9}
+    print(json.dumps(out), flush=True)
+
+
 def run_sweep(args):
     """Walk lengths uniform in 5-200 on the LJ-sized Chung-Lu graph; d x K x storage:
     the persistent engine (autotuned shape) against the plain engine (1/16 slice)."""
@@ -749,6 +786,7 @@ def main():
     ap.add_argument("--workload", default="lj-cl", choices=sorted(WORKLOADS))
     ap.add_argument("--skip-extras", action="store_true", help="only the timed bf16 steps (profiling runs)")
     ap.add_argument("--wpc", type=int, default=0, help="warps per CTA of the persistent engine (0 = autotune)")
+    ap.add_argument("--workers", type=int, default=0, help="persistent-engine workers (0 = default; profiling)")
     ap.add_argument("--auc", action="store_true", help="link-prediction AUC of every engine and the CPU reference")
     ap.add_argument("--auc-vertices", type=int, default=0, help="one fixture size (0 = every size)")
     ap.add_argument("--auc-workers", type=int, default=0, help="persistent-engine workers in --auc (0 = default)")
@@ -759,6 +797,8 @@ def main():
     ap.add_argument("--ingest", action="store_true", help="walk-text parse throughput (text GB/s, HBM roofline)")
     ap.add_argument("--eval", action="store_true", help="link-prediction scoring throughput (pairs/s, HBM roofline)")
     ap.add_argument("--files", action="store_true", help="walk file to trained model, timed end to end")
+    ap.add_argument("--walks", action="store_true", help="information-oriented walk generator throughput")
+    ap.add_argument("--walk-vertices", type=int, default=1_100_000)
     ap.add_argument("--adj-vertices", type=int, default=4_000_000)
     ap.add_argument("--adj-batches", type=int, default=200_000)
     args = ap.parse_args()
@@ -766,7 +806,8 @@ def main():
     if args.impl == "reference":
         return run_reference(args, wl)
     for flag, fn in (("auc", run_auc), ("mb_error", run_minibatch_error), ("sweep", run_sweep),
-                     ("adjoint", run_adjoint), ("ingest", run_ingest), ("eval", run_eval), ("files", run_files)):
+                     ("adjoint", run_adjoint), ("ingest", run_ingest), ("eval", run_eval), ("files", run_files),
+                     ("walks", run_walks)):
         if getattr(args, flag):
             import torch
 
@@ -793,7 +834,7 @@ def main():
     host_np = corpus_host.numpy()
 
     opt = sgns.default_options(iter=1, storage="bf16", engine="persistent", device=local, debug=0,
-                               warps_per_cta=args.wpc, **TRAIN)
+                               warps_per_cta=args.wpc, workers=args.workers, **TRAIN)
     tr = sgns.Trainer(opt)
     tr.set_vocab(counts)
     tr.upload(host_np)
