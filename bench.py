@@ -323,8 +323,8 @@ def auc_suite(sizes=None, persistent_workers=0, plain_workers=0, plain_all_seeds
     fixture (tests/golden/auc_sbm.json: the survey's configuration 2 -- 4-block SBM, 10%
     holdout, 10 information-oriented walks per vertex -- at 100k and 1.1M vertices, one
     graph/holdout/walk seed triple per case), against the CPU trainer's AUC recorded there.
-    The plain fp32 engine (one launch per step) runs on every seed at the smallest size and
-    on the first seed at larger sizes unless plain_all_seeds."""
+    The plain fp32 engine (one launch per step, minutes per corpus) runs on the first seed of
+    the largest size (configuration 2's drop-in), or on every case with plain_all_seeds."""
     import torch
     import sgns
     import synth
@@ -347,7 +347,7 @@ def auc_suite(sizes=None, persistent_workers=0, plain_workers=0, plain_all_seeds
             walks.append(info)
             counts = np.bincount(c[c >= 0], minlength=V).astype(np.int32)
             for name, eng, sto in arms:
-                if eng == "plain" and k > 0 and V != min(sizes) and not plain_all_seeds:
+                if eng == "plain" and not plain_all_seeds and (k > 0 or V != max(sizes)):
                     continue
                 w = plain_workers if eng == "plain" else persistent_workers
                 _, st, auc = _train_embedding(sgns, counts, c, V, eng, sto, 0, pos, neg, workers=w)
