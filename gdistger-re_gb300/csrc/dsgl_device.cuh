@@ -674,6 +674,81 @@ __device__ __forceinline__ void backward(int I, int O, int d, InPtr in_ptr, OutP
   __syncwarp();
 }
 
+// The same backward in one pass over the inputs, for steps in which no two inputs share a
+// row: input j's row is read for outputMd and then updated, and no later input reads it,
+// so every accumulator sees the same operands in the same order as backward<> above (md
+// sequential in j, each input's update summed over the outputs in the reference's order,
+// then added to the row).  One pass loads each input row and its coefficients once.
+template <int OM, int DCH, bool kT2Second = false, class InPtr, class OutPair>
+__device__ __forceinline__ void backward_merged(int I, int O, int d, InPtr in_ptr, OutPair out_pair,
+                                                const float2* corrP, float4 (&md)[OM][DCH]) {
+  typedef StepShape<OM> SS;
+  const int lane = lane_id();
+  const int d4 = d >> 2;
+  float2 olo[SS::OMP][DCH], ohi[SS::OMP][DCH];
+#pragma unroll
+  for (int pp = 0; pp < SS::NPAIR; pp++)
+#pragma unroll
+    for (int t = 0; t < DCH; t++) {
+      const int q = lane + 32 * t;
+      float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0;
+      if (2 * pp < O && q < d4) out_pair(pp, q, r0, r1);
+      olo[2 * pp][t] = make_float2(r0.x, r0.y);
+      ohi[2 * pp][t] = make_float2(r0.z, r0.w);
+      olo[2 * pp + 1][t] = make_float2(r1.x, r1.y);
+      ohi[2 * pp + 1][t] = make_float2(r1.z, r1.w);
+    }
+  float2 mlo[OM][DCH], mhi[OM][DCH];
+#pragma unroll
+  for (int i = 0; i < OM; i++)
+#pragma unroll
+    for (int t = 0; t < DCH; t++) mlo[i][t] = mhi[i][t] = make_float2(0.f, 0.f);
+  float4* x_next = I > 0 ? reinterpret_cast<float4*>(const_cast<float*>(in_ptr(0))) : nullptr;
+  for (int j = 0; j < I; j++) {
+    float4* x = x_next;
+    x_next = reinterpret_cast<float4*>(const_cast<float*>(in_ptr(j + 1 < I ? j + 1 : j)));
+    const float4* cj = reinterpret_cast<const float4*>(corrP + j * SS::CS);
+    float2 c[SS::OMP];
+#pragma unroll
+    for (int q = 0; q < SS::NPAIR; q++) {
+      const float4 v = cj[q];
+      c[2 * q] = make_float2(v.x, v.y);
+      c[2 * q + 1] = make_float2(v.z, v.w);
+    }
+#pragma unroll
+    for (int t = 0; t < DCH; t++) {
+      const int q = lane + 32 * t;
+      if (q < d4) {
+        const float4 xv = x[q];
+        const float2 xl = make_float2(xv.x, xv.y), xh = make_float2(xv.z, xv.w);
+#pragma unroll
+        for (int i = 0; i < OM; i++)
+          if (i < O) {
+            mlo[i][t] = ffma2(c[i], xl, mlo[i][t]);
+            mhi[i][t] = ffma2(c[i], xh, mhi[i][t]);
+          }
+        float2 al = make_float2(0.f, 0.f), ah = al;
+#pragma unroll
+        for (int k = 0; k < OM; k++) {
+          const int i = !kT2Second ? k : (k == 0 ? 0 : (k == OM - 1 ? 1 : k + 1));
+          const bool used = !kT2Second ? k < O : (k == 0 || k == OM - 1 || k + 1 < O);
+          if (used) {
+            al = ffma2(c[i], olo[i][t], al);
+            ah = ffma2(c[i], ohi[i][t], ah);
+          }
+        }
+        const float2 lo = fadd2(xl, al), hi = fadd2(xh, ah);
+        x[q] = make_float4(lo.x, lo.y, hi.x, hi.y);
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < OM; i++)
+#pragma unroll
+    for (int t = 0; t < DCH; t++) md[i][t] = make_float4(mlo[i][t].x, mlo[i][t].y, mhi[i][t].x, mhi[i][t].y);
+  __syncwarp();
+}
+
 // Stores the step's output rows from registers in the interleaved layout (see StepShape).
 template <int OM, int DCH>
 __device__ __forceinline__ void store_out_interleaved(const float4 (&v)[OM][DCH], int O, int d, float* outI) {

@@ -185,6 +185,7 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
   // the variant with registers to spare for them across the transitions does this (bf16,
   // d <= 128, K <= 5: +3.7%; the fp32 rows are twice the registers and spill, -10%).
   constexpr bool kPrefetchRows = S == STORE_BF16 && DCH == 1 && OM == 7;
+  constexpr bool kMergedBackward = true;
   typename RowIO<S>::Raw ov[OM][DCH];
   bool ov_ready = false;
   int O_next = 0;
@@ -412,7 +413,15 @@ __global__ void __launch_bounds__(256) window_engine_kernel(TrainParams p) {
       r1 = 2 * pp + 1 < O ? reinterpret_cast<const float4*>(out_rows + (size_t)(2 * pp + 1) * DP)[q]
                           : make_float4(0.f, 0.f, 0.f, 0.f);
     };
-    backward<OM, DCH, true>(I, O, d, in_ptr, out_pair, corrP, md, add_to_input(in_ptr));
+    // one pass over the inputs when no two of them share a window row (at most 32
+    // inputs, distinct slots); otherwise outputMd first, then the updates
+    bool merged = false;
+    if (kMergedBackward && I <= 32) {
+      const int r = lane < I ? in_row[lane] : -1 - lane;
+      merged = !__any_sync(kFull, __popc(__match_any_sync(kFull, r)) > 1);
+    }
+    if (merged) backward_merged<OM, DCH, true>(I, O, d, in_ptr, out_pair, corrP, md);
+    else backward<OM, DCH, true>(I, O, d, in_ptr, out_pair, corrP, md, add_to_input(in_ptr));
     {  // Woh += outputMd: target 1, target 2, then each negative (aliases follow that order)
       uint64_t e1 = 0, e2 = 0, en = 0;
       if (S == STORE_BF16) {
