@@ -14,7 +14,11 @@
 // the compact gradient rows are zeroed, and each minibatch adds its row gradients into
 // its rows' slots.
 //
-// Kernels (one warp per minibatch, four per block):
+// Gradient kernels.  adjoint_pipe_kernel (tables whose rows are whole 16-byte chunks at
+// 16-byte aligned addresses) runs persistent warps that copy the next minibatch's rows
+// into a second shared-memory buffer with cp.async while the current one computes (its
+// comment below gives the details).  adjoint_kernel takes every other shape, one warp per
+// minibatch and four per block:
 //   * rows are staged in shared memory with 16-byte loads (8 bytes per 4 bf16 elements),
 //     input rows padded to a stride of d + 4 words so lanes reading different rows at the
 //     same column fall in different banks;
@@ -389,6 +393,311 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) adjoint_kernel(
   if (lane == 0 && loss != 0) atomicAdd(&loss_parts[b & 255], (double)loss);
 }
 
+// ---- pipelined gradient kernel: tables whose rows are whole 16-byte chunks ----------------
+// Persistent warps: warp g runs minibatches g, g + S, g + 2S, ... (S = warps in the grid).
+// The rows of the next minibatch are copied into the warp's second row buffer with
+// cp.async (16 bytes per lane and copy, cached in L2 only) while the current one computes,
+// so the row gathers leave the dependent chain.  The next minibatch's ids are loaded at
+// the top of an iteration, its gradient slots after the forward, and the extents one
+// minibatch further ahead.  Rows stay in their storage format in the buffers (row stride
+// = row bytes + 16, so lanes reading different rows at one column hit different banks);
+// the output rows are widened once into an fp32 (fp64) copy for the forward's broadcast
+// reads.  Sums keep the order of adjoint_kernel except the forward's dot products, which
+// run as an even and an odd partial sum for fp32.
+
+template <int DT> struct Pipe;
+template <> struct Pipe<0> {  // fp32 rows: 4 elements per 16 bytes
+  typedef float T;
+  static constexpr int kBytes = 4;
+  __device__ static __forceinline__ void chunk4(const unsigned char* p, float (&v)[4]) {  // 4 elements at p
+    const float4 f = *reinterpret_cast<const float4*>(p);
+    v[0] = f.x, v[1] = f.y, v[2] = f.z, v[3] = f.w;
+  }
+};
+template <> struct Pipe<1> {  // bf16 rows
+  typedef float T;
+  static constexpr int kBytes = 2;
+  __device__ static __forceinline__ void chunk4(const unsigned char* p, float (&v)[4]) {
+    const uint2 u = *reinterpret_cast<const uint2*>(p);
+    v[0] = __uint_as_float(u.x << 16), v[1] = __uint_as_float(u.x & 0xFFFF0000u);
+    v[2] = __uint_as_float(u.y << 16), v[3] = __uint_as_float(u.y & 0xFFFF0000u);
+  }
+};
+template <> struct Pipe<2> {  // fp64 rows
+  typedef double T;
+  static constexpr int kBytes = 8;
+  __device__ static __forceinline__ void chunk4(const unsigned char* p, double (&v)[4]) {
+    const double2 a = reinterpret_cast<const double2*>(p)[0], b = reinterpret_cast<const double2*>(p)[1];
+    v[0] = a.x, v[1] = a.y, v[2] = b.x, v[3] = b.y;
+  }
+};
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Per-warp shared memory of the pipelined kernel, in bytes (every region 16-byte aligned):
+// two row buffers of (imax + omax) rows, the widened output rows, the coefficients
+// (imax rows of round4(omax)) and the gradient slots.
+struct PipeLayout {
+  int RS, CS, buf, ofp, coef, slot, bytes;
+};
+__host__ __device__ inline PipeLayout pipe_layout(int dtype, int d, int imax, int omax) {
+  const int eb = dtype == 2 ? 8 : dtype == 1 ? 2 : 4, tb = dtype == 2 ? 8 : 4;
+  PipeLayout L;
+  L.RS = d * eb + 16;
+  L.CS = (omax + 3) & ~3;
+  L.buf = (imax + omax) * L.RS;
+  L.ofp = 2 * L.buf;
+  L.coef = L.ofp + omax * d * tb;
+  L.slot = L.coef + imax * L.CS * tb;
+  L.bytes = (L.slot + 4 * (imax + omax) + 15) & ~15;
+  return L;
+}
+
+// minibatch extents: i0, I, o0, O, first
+struct Extent {
+  int i0, I, o0, O, first;
+};
+__device__ __forceinline__ Extent load_extent(int b, int n, const int32_t* in_ptr, const int32_t* in_first,
+                                              const int32_t* out_ptr) {
+  Extent e{0, 0, 0, 0, 0};
+  if (b < n) {
+    e.i0 = in_ptr[b], e.I = in_ptr[b + 1] - e.i0, e.o0 = out_ptr[b], e.O = out_ptr[b + 1] - e.o0;
+    e.first = in_first[b];
+  }
+  return e;
+}
+// lane l holds the ids of rows l, l + 32 and l + 64 (inputs, then outputs)
+__device__ __forceinline__ void load_ids(const Extent& e, bool valid, const int32_t* in_ids, const int32_t* out_ids,
+                                         int (&id)[3]) {
+  const int lane = lane_id();
+#pragma unroll
+  for (int m = 0; m < 3; m++) {
+    const int j = lane + 32 * m;
+    id[m] = !valid ? 0 : j < e.I ? in_ids[e.i0 + j] : j < e.I + e.O ? out_ids[e.o0 + j - e.I] : 0;
+  }
+}
+__device__ __forceinline__ int row_id(const int (&id)[3], int r) {  // uniform or per-lane r < 96
+  const int a = __shfl_sync(kFull, id[0], r & 31), b = __shfl_sync(kFull, id[1], r & 31),
+            c = __shfl_sync(kFull, id[2], r & 31);
+  return r < 32 ? a : r < 64 ? b : c;
+}
+
+template <int DT, int OMX>
+__global__ void __launch_bounds__(256) adjoint_pipe_kernel(
+    int d, int n, int imax, int omax, const int32_t* in_ptr, const int32_t* in_ids, const int32_t* in_first,
+    const int32_t* out_ptr, const int32_t* out_ids, const int32_t* out_meta, const void* wih, const void* woh,
+    int64_t V, const int32_t* incl_in, const int32_t* incl_out, typename Pipe<DT>::T* g_in,
+    typename Pipe<DT>::T* g_out, double* loss_parts) {
+  typedef typename Pipe<DT>::T T;
+  constexpr int EB = Pipe<DT>::kBytes;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = lane_id(), wpb = blockDim.x >> 5;
+  const int gw = blockIdx.x * wpb + (threadIdx.x >> 5), S = gridDim.x * wpb;
+  const PipeLayout L = pipe_layout(DT, d, imax, omax);
+  unsigned char* wbase = smem_raw + (size_t)(threadIdx.x >> 5) * L.bytes;
+  T* ofp = reinterpret_cast<T*>(wbase + L.ofp);
+  T* coef = reinterpret_cast<T*>(wbase + L.coef);
+  int32_t* slot = reinterpret_cast<int32_t*>(wbase + L.slot);
+  const int row_bytes = d * EB, C = row_bytes >> 4;  // 16-byte chunks per row
+  const int rpi = C <= 32 ? 32 / C : 1, lane_row = C <= 32 ? lane / C : 0, lane_chunk = C <= 32 ? lane % C : 0;
+  const unsigned char* tin = static_cast<const unsigned char*>(wih);
+  const unsigned char* tout = static_cast<const unsigned char*>(woh);
+
+  // sizes within this launch's buffers and ids inside [0, V) (the marking pass flagged
+  // any minibatch that is not; it is skipped)
+  auto extent_ok = [&](const Extent& e) {
+    return e.i0 >= 0 && e.o0 >= 0 && e.I >= 0 && e.I <= imax && e.O >= 0 && e.O <= omax && e.O <= OMX &&
+           e.first >= 0 && e.first <= e.I;
+  };
+  auto ids_ok = [&](const Extent& e, const int (&id)[3]) {
+    bool ok = true;
+#pragma unroll
+    for (int m = 0; m < 3; m++) ok &= lane + 32 * m >= e.I + e.O || (id[m] >= 0 && id[m] < V);
+    return __all_sync(kFull, ok);
+  };
+  auto issue_copies = [&](const Extent& e, const int (&id)[3], unsigned char* buf) {
+    const int R = e.I + e.O;
+    if (C <= 32) {
+      for (int r0 = 0; r0 < R; r0 += rpi) {
+        const int r = r0 + lane_row;
+        const int rid = row_id(id, r);
+        if (lane_row < rpi && r < R)
+          cp_async16(buf + (size_t)r * L.RS + 16 * lane_chunk,
+                     (r < e.I ? tin : tout) + (int64_t)rid * row_bytes + 16 * lane_chunk);
+      }
+    } else {
+      for (int r = 0; r < R; r++) {
+        const int rid = row_id(id, r);
+        for (int k = lane; k < C; k += 32)
+          cp_async16(buf + (size_t)r * L.RS + 16 * k, (r < e.I ? tin : tout) + (int64_t)rid * row_bytes + 16 * k);
+      }
+    }
+    cp_async_commit();
+  };
+  auto load_slots = [&](const Extent& e, const int (&id)[3], int (&sl)[3]) {
+#pragma unroll
+    for (int m = 0; m < 3; m++) {
+      const int j = lane + 32 * m;
+      sl[m] = j < e.I ? incl_in[id[m]] - 1 : j < e.I + e.O ? incl_out[id[m]] - 1 : 0;
+    }
+  };
+
+  // prologue: the first minibatch's rows in flight, the second one's extent loaded
+  int b = gw;
+  Extent cur = load_extent(b, n, in_ptr, in_first, out_ptr);
+  bool cur_ok = b < n && extent_ok(cur);
+  int idc[3], slc[3] = {0, 0, 0};
+  load_ids(cur, cur_ok, in_ids, out_ids, idc);
+  cur_ok = cur_ok && ids_ok(cur, idc);
+  if (cur_ok) {
+    issue_copies(cur, idc, wbase);
+    load_slots(cur, idc, slc);
+  }
+  Extent nxt = load_extent(b + S, n, in_ptr, in_first, out_ptr);
+  int s = 0;
+  T loss = 0;
+  const int nq = d >> 2;
+  while (b < n) {
+    const int bn = b + S;
+    bool nxt_ok = bn < n && extent_ok(nxt);
+    int idn[3], sln[3] = {0, 0, 0};
+    load_ids(nxt, nxt_ok, in_ids, out_ids, idn);
+    const Extent nn = load_extent(bn + S, n, in_ptr, in_first, out_ptr);
+    unsigned char* buf = wbase + (size_t)s * L.buf;
+    cp_async_wait_all();
+    if (cur_ok) {
+#pragma unroll
+      for (int m = 0; m < 3; m++)
+        if (lane + 32 * m < cur.I + cur.O) slot[lane + 32 * m] = slc[m];
+    }
+    __syncwarp();
+    const int I = cur.I, O = cur.O;
+    if (cur_ok) {
+      // widen the output rows once (column-parallel)
+      for (int i = 0; i < O; i++)
+        for (int q = lane; q < nq; q += 32) {
+          T v[4];
+          Pipe<DT>::chunk4(buf + (size_t)(I + i) * L.RS + 4 * q * EB, v);
+          sts4(ofp + (size_t)i * d + 4 * q, v);
+        }
+      __syncwarp();
+      // dot products, one lane per input
+      for (int j0 = 0; j0 < I; j0 += 32) {
+        const int j = j0 + lane;
+        const unsigned char* xr = buf + (size_t)(j < I ? j : 0) * L.RS;
+        T f[OMX];
+        if constexpr (DT == 2) {
+#pragma unroll
+          for (int i = 0; i < OMX; i++) f[i] = 0;
+          for (int k = 0; k < d; k += 4) {
+            T xv[4];
+            Pipe<DT>::chunk4(xr + k * EB, xv);
+#pragma unroll
+            for (int i = 0; i < OMX; i++)
+              if (i < O) {
+                T ov[4];
+                lds4(ofp + (size_t)i * d + k, ov);
+#pragma unroll
+                for (int t = 0; t < 4; t++) f[i] = fma_t(ov[t], xv[t], f[i]);
+              }
+          }
+        } else {
+          // 16 bytes of the input row per step: 8 bf16 or 4 fp32 elements, even and odd
+          // partial sums in packed fp32 pairs
+          constexpr int VK = 16 / EB;
+          float2 fp[OMX];
+#pragma unroll
+          for (int i = 0; i < OMX; i++) fp[i] = make_float2(0.f, 0.f);
+          for (int k = 0; k < d; k += VK) {
+            float xv[VK];
+            Pipe<DT>::chunk4(xr + k * EB, *reinterpret_cast<float(*)[4]>(xv));
+            if constexpr (VK == 8) Pipe<DT>::chunk4(xr + k * EB + 8, *reinterpret_cast<float(*)[4]>(xv + 4));
+#pragma unroll
+            for (int i = 0; i < OMX; i++)
+              if (i < O) {
+#pragma unroll
+                for (int h = 0; h < VK; h += 4) {
+                  const float4 o4 = *reinterpret_cast<const float4*>(ofp + (size_t)i * d + k + h);
+                  fp[i] = __ffma2_rn(make_float2(o4.x, o4.y), make_float2(xv[h], xv[h + 1]), fp[i]);
+                  fp[i] = __ffma2_rn(make_float2(o4.z, o4.w), make_float2(xv[h + 2], xv[h + 3]), fp[i]);
+                }
+              }
+          }
+#pragma unroll
+          for (int i = 0; i < OMX; i++) f[i] = __fadd_rn(fp[i].x, fp[i].y);
+        }
+        if (j < I) {
+#pragma unroll
+          for (int i = 0; i < OMX; i++)
+            if (i < O) {
+              const int label = j < cur.first ? (i == 0) : (i == O - 1);
+              T c;
+              pair_terms(f[i], label, (T)out_meta[cur.o0 + i], loss, c);
+              coef[(size_t)j * L.CS + i] = c;
+            }
+        }
+      }
+      __syncwarp();
+    }
+    // the next minibatch's rows into the other buffer, its slots behind them
+    nxt_ok = nxt_ok && ids_ok(nxt, idn);
+    if (nxt_ok) {
+      issue_copies(nxt, idn, wbase + (size_t)(s ^ 1) * L.buf);
+      load_slots(nxt, idn, sln);
+    }
+    if (cur_ok) {
+      // gradient rows, column-parallel: dL/dWih[x_j] = sum_i c_ij Woh[o_i] (order i) and
+      // dL/dWoh[o_i] = sum_j c_ij Wih[x_j] (order j)
+      for (int q = lane; q < nq; q += 32) {
+        T ov[OMX][4], ao[OMX][4];
+#pragma unroll
+        for (int i = 0; i < OMX; i++)
+#pragma unroll
+          for (int t = 0; t < 4; t++) ov[i][t] = ao[i][t] = 0;
+#pragma unroll
+        for (int i = 0; i < OMX; i++)
+          if (i < O) lds4(ofp + (size_t)i * d + 4 * q, ov[i]);
+        for (int j = 0; j < I; j++) {
+          T xv[4];
+          Pipe<DT>::chunk4(buf + (size_t)j * L.RS + 4 * q * EB, xv);
+          const T* cj = coef + (size_t)j * L.CS;
+          T ai[4] = {0, 0, 0, 0};
+#pragma unroll
+          for (int i = 0; i < OMX; i++)
+            if (i < O) {
+              const T c = cj[i];
+#pragma unroll
+              for (int t = 0; t < 4; t++) {
+                ai[t] = fma_t(c, ov[i][t], ai[t]);
+                ao[i][t] = fma_t(c, xv[t], ao[i][t]);
+              }
+            }
+          atomic_add4(g_in + (size_t)slot[j] * d + 4 * q, ai);
+        }
+#pragma unroll
+        for (int i = 0; i < OMX; i++)
+          if (i < O) atomic_add4(g_out + (size_t)slot[I + i] * d + 4 * q, ao[i]);
+      }
+    }
+    __syncwarp();
+    b = bn;
+    cur = nxt;
+    nxt = nn;
+    cur_ok = nxt_ok;
+#pragma unroll
+    for (int m = 0; m < 3; m++) idc[m] = idn[m], slc[m] = sln[m];
+    s ^= 1;
+  }
+  cp_async_wait_all();
+  for (int sh = 16; sh > 0; sh >>= 1) loss += __shfl_xor_sync(kFull, loss, sh);
+  if (lane == 0 && loss != 0) atomicAdd(&loss_parts[gw & 255], (double)loss);
+}
+
 __global__ void finish_loss_kernel(const double* parts, double* loss) {
   double v = parts[threadIdx.x];  // 256 threads
   for (int sh = 16; sh > 0; sh >>= 1) v += __shfl_xor_sync(kFull, v, sh);
@@ -500,6 +809,44 @@ cudaError_t launch_adjoint(int dtype, int d, int n, int64_t V, int imax, int oma
     else SGNS_ADJ_LAUNCH1(DT, VW, kOMax, TT);         \
   } while (0)
   const bool v4 = d % 4 == 0;
+  // the pipelined kernel when rows are whole 16-byte chunks at 16-byte aligned addresses
+  const int eb = dtype == 2 ? 8 : dtype == 1 ? 2 : 4;
+  const PipeLayout PL = pipe_layout(dtype, d, imax, omax);
+  if (v4 && (d * eb) % 16 == 0 && ((uintptr_t)wih & 15) == 0 && ((uintptr_t)woh & 15) == 0 &&
+      PL.bytes <= 232448) {
+    const int pw = std::max(1, std::min(8, 232448 / PL.bytes));
+    const size_t psmem = (size_t)pw * PL.bytes;
+    int dev = 0, sms = 0;
+    if ((e = cudaGetDevice(&dev)) || (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev))) return e;
+#define SGNS_ADJ_PIPE1(DT, OMX, TT)                                                                             \
+  do {                                                                                                          \
+    if ((e = cudaFuncSetAttribute(adjoint_pipe_kernel<DT, OMX>, cudaFuncAttributeMaxDynamicSharedMemorySize,     \
+                                  (int)psmem)))                                                                 \
+      return e;                                                                                                 \
+    int per_sm = 0;                                                                                             \
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adjoint_pipe_kernel<DT, OMX>, 32 * pw,      \
+                                                           psmem)))                                             \
+      return e;                                                                                                 \
+    const unsigned pb = (unsigned)std::max<int64_t>(                                                            \
+        1, std::min<int64_t>((n + pw - 1) / pw, (int64_t)sms * std::max(per_sm, 1)));                           \
+    adjoint_pipe_kernel<DT, OMX><<<pb, 32 * pw, psmem, s>>>(d, n, imax, omax, in_ptr, in_ids, in_first, out_ptr,  \
+                                                            out_ids, out_meta, wih, woh, V, incl_in, incl_out,   \
+                                                            static_cast<TT*>(grad_in),                          \
+                                                            static_cast<TT*>(grad_out), parts);                 \
+  } while (0)
+#define SGNS_ADJ_PIPE(DT, TT)                  \
+  do {                                         \
+    if (omax <= 7) SGNS_ADJ_PIPE1(DT, 7, TT);  \
+    else SGNS_ADJ_PIPE1(DT, kOMax, TT);        \
+  } while (0)
+    if (dtype == 2) SGNS_ADJ_PIPE(2, double);
+    else if (dtype == 1) SGNS_ADJ_PIPE(1, float);
+    else SGNS_ADJ_PIPE(0, float);
+#undef SGNS_ADJ_PIPE
+#undef SGNS_ADJ_PIPE1
+    finish_loss_kernel<<<1, 256, 0, s>>>(parts, loss);
+    return cudaGetLastError();
+  }
   if (dtype == 2) {
     if (v4) SGNS_ADJ_LAUNCH(2, 4, double);
     else SGNS_ADJ_LAUNCH(2, 1, double);

@@ -103,9 +103,25 @@ SGNS_HD uint64_t mix64(uint64_t z) {  // SplitMix64 finaliser (Steele, Lea, Floo
 SGNS_HD uint64_t sr_event_key(uint64_t seed, int kind, uint32_t worker, uint64_t step) {
   return mix64(seed ^ ((uint64_t)kind << 56) ^ ((uint64_t)worker << 34) ^ step);
 }
-// 64 random bits for the 4 consecutive columns 4*col4 .. 4*col4+3 of one row
+// 64 random bits for the 4 consecutive columns 4*col4 .. 4*col4+3 of one row, from the
+// event key ev (one SplitMix64 output per write event):
+//   h  = fmix32(lo32(ev) ^ (row * 0x9E3779B1 + col4 * 0x85EBCA77))   (murmur3's 32-bit
+//        finaliser, Appleby 2011; constants of Wellons' low-bias variant),
+//   h2 = high 32 bits of the 64-bit product (h ^ hi32(ev)) * 0xCC9E2D51,
+//   bits = h2 << 32 | h  (columns 4q, 4q+1 take h; 4q+2, 4q+3 take h2).
+// About a third of the instructions of a 64-bit finaliser per chunk, on the write-back
+// path of every output row of every step.
+SGNS_HD uint32_t fmix32(uint32_t h) {
+  h ^= h >> 16;
+  h *= 0x7FEB352Du;
+  h ^= h >> 15;
+  h *= 0x846CA68Bu;
+  return h ^ (h >> 16);
+}
 SGNS_HD uint64_t sr_bits4(uint64_t ev, uint32_t row, uint32_t col4) {
-  return mix64(ev ^ ((uint64_t)row << 8) ^ (uint64_t)col4);
+  const uint32_t h = fmix32((uint32_t)ev ^ (row * 0x9E3779B1u + col4 * 0x85EBCA77u));
+  const uint32_t h2 = (uint32_t)(((uint64_t)(h ^ (uint32_t)(ev >> 32)) * 0xCC9E2D51u) >> 32);
+  return ((uint64_t)h2 << 32) | h;
 }
 SGNS_HD float bf16_bits_to_f32(uint16_t b) {
   uint32_t u = (uint32_t)b << 16;

@@ -64,9 +64,23 @@ inline uint64_t mix64(uint64_t z) {
 inline uint64_t sr_event_key(uint64_t seed, int kind, uint32_t worker, uint64_t step) {
   return mix64(seed ^ ((uint64_t)kind << 56) ^ ((uint64_t)worker << 34) ^ step);
 }
+// 16 random bits for one column: columns 4q, 4q+1 take the low and high halves of
+// h = fmix32(lo32(ev) ^ (row * 0x9E3779B1 + q * 0x85EBCA77)) (murmur3's 32-bit finaliser
+// with Wellons' low-bias constants), columns 4q+2, 4q+3 those of
+// h2 = hi32((h ^ hi32(ev)) * 0xCC9E2D51)
+inline uint32_t fmix32(uint32_t h) {
+  h ^= h >> 16;
+  h *= 0x7FEB352Du;
+  h ^= h >> 15;
+  h *= 0x846CA68Bu;
+  return h ^ (h >> 16);
+}
 inline uint32_t sr_bits16(uint64_t ev, uint32_t row, int col) {
-  uint64_t h = mix64(ev ^ ((uint64_t)row << 8) ^ (uint64_t)(col >> 2));
-  return (uint32_t)(h >> ((col & 3) * 16)) & 0xFFFFu;
+  const uint32_t q = (uint32_t)(col >> 2);
+  const uint32_t h = fmix32((uint32_t)ev ^ (row * 0x9E3779B1u + q * 0x85EBCA77u));
+  const uint32_t h2 = (uint32_t)(((uint64_t)(h ^ (uint32_t)(ev >> 32)) * 0xCC9E2D51u) >> 32);
+  const uint64_t bits = ((uint64_t)h2 << 32) | h;
+  return (uint32_t)(bits >> ((col & 3) * 16)) & 0xFFFFu;
 }
 inline float bf16_to_f32(uint16_t b) {
   uint32_t u = (uint32_t)b << 16;

@@ -178,3 +178,46 @@ def test_sparse_rows_ascending_and_unique(sgns_lib):
     assert ni == len(np.unique(mb["in_ids"].cpu().numpy())) and (np.diff(ids) > 0).all()
     ids = go_ids[:no].cpu().numpy()
     assert no == len(np.unique(mb["out_ids"].cpu().numpy())) and (np.diff(ids) > 0).all()
+
+
+def dense_adjoint(code, wih, woh, mb):
+    """loss and dense (fp64) gradients from the library's sparse adjoint; code = table type
+    (0 fp32, 1 bf16, 2 fp64)."""
+    d = wih.shape[1]
+    gdt = torch.float64 if code == 2 else torch.float32
+    n_in, n_out = mb["in_ids"].numel(), mb["out_ids"].numel()
+    loss = torch.zeros(1, dtype=torch.float64, device="cuda")
+    gi_ids = torch.empty(n_in, dtype=torch.int32, device="cuda")
+    go_ids = torch.empty(n_out, dtype=torch.int32, device="cuda")
+    gi = torch.empty((n_in, d), dtype=gdt, device="cuda")
+    go = torch.empty((n_out, d), dtype=gdt, device="cuda")
+    ni, no = sgns.loss_adjoint(code, d, mb["V"], mb["in_ptr"], mb["in_ids"], mb["in_first"], mb["out_ptr"],
+                               mb["out_ids"], mb["out_meta"], wih.data_ptr(), woh.data_ptr(), loss, gi_ids, gi,
+                               go_ids, go)
+    dw = torch.zeros(wih.shape, dtype=torch.float64, device="cuda").index_add_(0, gi_ids[:ni].long(),
+                                                                               gi[:ni].double())
+    do = torch.zeros(woh.shape, dtype=torch.float64, device="cuda").index_add_(0, go_ids[:no].long(),
+                                                                               go[:no].double())
+    return loss.item(), dw, do
+
+
+# (table type, d, negatives, window): rows of whole 16-byte chunks take the pipelined
+# kernel (up to 40 inputs and 12 outputs per minibatch, rows of 4 to 64 chunks); d = 36
+# bf16 (72-byte rows) and d = 30 fp32 take the general one
+@pytest.mark.parametrize("code,d,K,w", [(1, 128, 5, 10), (1, 256, 10, 10), (0, 256, 10, 5), (0, 64, 5, 10),
+                                        (2, 32, 10, 10), (1, 36, 5, 10), (0, 30, 5, 5)])
+def test_adjoint_kernels_against_fp64_autograd(sgns_lib, code, d, K, w):
+    mb = sbm_minibatches(n=48, K=K, w=w, seed=11 + d + K)
+    dt = {0: torch.float32, 1: torch.bfloat16, 2: torch.float64}[code]
+    w64, o64 = tables(mb["V"], d, torch.float64, seed=5)
+    wih, woh = w64.to(dt), o64.to(dt)
+    loss, dw, do = dense_adjoint(code, wih, woh, mb)
+    a = wih.double().requires_grad_(True)
+    b = woh.double().requires_grad_(True)
+    ref = torch_loss(a, b, mb)
+    ref.backward()
+    tol = 1e-12 if code == 2 else 2e-6
+    assert abs(loss - ref.item()) <= tol * abs(ref.item())
+    for got, want in ((dw, a.grad), (do, b.grad)):
+        err = (got - want).abs().max().item()
+        assert err <= tol * want.abs().max().item() * 10, (err, want.abs().max().item())

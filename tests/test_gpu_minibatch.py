@@ -95,16 +95,35 @@ def mix64(z):
     return z ^ (z >> 31)
 
 
+M32 = (1 << 32) - 1
+
+
+def fmix32(h):
+    h ^= h >> 16
+    h = (h * 0x7FEB352D) & M32
+    h ^= h >> 15
+    h = (h * 0x846CA68B) & M32
+    return h ^ (h >> 16)
+
+
+def sr_bits4(key, r, q):
+    """64 bits for columns 4q..4q+3 of row r: h = fmix32(lo32(key) ^ (r * 0x9E3779B1 +
+    q * 0x85EBCA77)), h2 = hi32((h ^ hi32(key)) * 0xCC9E2D51), bits = h2 << 32 | h."""
+    h = fmix32((key & M32) ^ ((r * 0x9E3779B1 + q * 0x85EBCA77) & M32))
+    h2 = ((h ^ (key >> 32)) * 0xCC9E2D51) >> 32
+    return (h2 << 32) | h
+
+
 def sr_rows(v, seed, kind, b):
     """The trainers' write-back rule on fp32 rows v [rows, d]: column 4q + j of row r takes
-    bits [16j, 16j + 16) of mix64(key ^ (r << 8) ^ q), key = mix64(seed ^ (kind << 56) ^ b);
+    bits [16j, 16j + 16) of sr_bits4(key, r, q), key = mix64(seed ^ (kind << 56) ^ b);
     stored bits = (bits(x) + r16) >> 16."""
     key = mix64((seed ^ (kind << 56) ^ b) & M64)
     u = v.astype(np.float32).view(np.uint32).astype(np.uint64)
     out = np.zeros(v.shape, np.uint16)
     for r in range(v.shape[0]):
         for q in range(v.shape[1] // 4):
-            bits = mix64(key ^ ((r << 8) & M64) ^ q)
+            bits = sr_bits4(key, r, q)
             for j in range(4):
                 r16 = (bits >> (16 * j)) & 0xFFFF
                 out[r, 4 * q + j] = (int(u[r, 4 * q + j]) + r16) >> 16
