@@ -16,8 +16,8 @@
 //
 // Gradient kernels.  adjoint_pipe_kernel (tables whose rows are whole 16-byte chunks at
 // 16-byte aligned addresses) runs persistent warps that copy the next minibatch's rows
-// into a second shared-memory buffer with cp.async while the current one computes (its
-// comment below gives the details).  adjoint_kernel takes every other shape, one warp per
+// into shared memory with cp.async while the current one computes, when both fit in the
+// warp's ring of rows (its comment below gives the details).  adjoint_kernel takes every other shape, one warp per
 // minibatch and four per block:
 //   * rows are staged in shared memory with 16-byte loads (8 bytes per 4 bf16 elements),
 //     input rows padded to a stride of d + 4 words so lanes reading different rows at the
@@ -101,27 +101,29 @@ __device__ __forceinline__ void atomic_add4(double* dst, const double (&v)[4]) {
   for (int k = 0; k < 4; k++) atomicAdd(dst + k, v[k]);
 }
 
-// Marks the rows of every minibatch (one thread per minibatch), checks its extents and
-// records the largest input and output counts (dims[0], dims[1]).
+// Marks the rows of every minibatch (one warp per minibatch, one lane per id), checks its
+// extents and records the largest input and output counts (dims[0], dims[1]).
 __global__ void mark_rows_kernel(int n, const int32_t* in_ptr, const int32_t* in_ids, const int32_t* in_first,
                                  const int32_t* out_ptr, const int32_t* out_ids, int64_t V, int32_t* mark_in,
                                  int32_t* mark_out, int32_t* status, int32_t* dims) {
+  const int lane = lane_id();
+  const int warps = (int)((gridDim.x * blockDim.x) >> 5);
   int imax = 0, omax = 0;
-  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < n; b += gridDim.x * blockDim.x) {
+  for (int b = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); b < n; b += warps) {
     const int i0 = in_ptr[b], i1 = in_ptr[b + 1], o0 = out_ptr[b], o1 = out_ptr[b + 1];
     if (i0 < 0 || o0 < 0 || i1 - i0 < 0 || i1 - i0 > kIMax || o1 - o0 < 0 || o1 - o0 > kOMax ||
         in_first[b] < 0 || in_first[b] > i1 - i0) {
-      atomicOr(status, kBadSize);
+      if (lane == 0) atomicOr(status, kBadSize);
       continue;
     }
     imax = max(imax, i1 - i0);
     omax = max(omax, o1 - o0);
-    for (int t = i0; t < i1; t++) {
+    for (int t = i0 + lane; t < i1; t += 32) {
       const int32_t r = in_ids[t];
       if (r < 0 || r >= V) atomicOr(status, kBadId);
       else mark_in[r] = 1;
     }
-    for (int t = o0; t < o1; t++) {
+    for (int t = o0 + lane; t < o1; t += 32) {
       const int32_t r = out_ids[t];
       if (r < 0 || r >= V) atomicOr(status, kBadId);
       else mark_out[r] = 1;
@@ -395,11 +397,15 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) adjoint_kernel(
 
 // ---- pipelined gradient kernel: tables whose rows are whole 16-byte chunks ----------------
 // Persistent warps: warp g runs minibatches g, g + S, g + 2S, ... (S = warps in the grid).
-// The rows of the next minibatch are copied into the warp's second row buffer with
-// cp.async (16 bytes per lane and copy, cached in L2 only) while the current one computes,
-// so the row gathers leave the dependent chain.  The next minibatch's ids are loaded at
-// the top of an iteration, its gradient slots after the forward, and the extents one
-// minibatch further ahead.  Rows stay in their storage format in the buffers (row stride
+// Each warp holds a ring of imax + omax rows (one largest minibatch).  After the forward,
+// the next minibatch's rows are copied with cp.async (16 bytes per lane and copy, cached in
+// L2 only) behind the current ones or at the ring's start when they fit beside them, so
+// their gathers overlap the backward; otherwise they are copied once the backward is
+// done.  A ring of one minibatch leaves room for more resident warps, which measured
+// faster than a second full buffer (12 warps per SM against 7 at d = 128, bf16, K = 5:
+// 2.08 against 2.86 ms per call on the 4M-vertex case).  The next minibatch's ids are
+// loaded at the top of an iteration, its gradient slots with its copies, and the extents
+// one minibatch further ahead.  Rows stay in their storage format in the ring (row stride
 // = row bytes + 16, so lanes reading different rows at one column hit different banks);
 // the output rows are widened once into an fp32 (fp64) copy for the forward's broadcast
 // reads.  Sums keep the order of adjoint_kernel except the forward's dot products, which
@@ -440,18 +446,18 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 // Per-warp shared memory of the pipelined kernel, in bytes (every region 16-byte aligned):
-// two row buffers of (imax + omax) rows, the widened output rows, the coefficients
+// the ring of `ring` rows, the widened output rows, the coefficients
 // (imax rows of round4(omax)) and the gradient slots.
 struct PipeLayout {
   int RS, CS, buf, ofp, coef, slot, bytes;
 };
-__host__ __device__ inline PipeLayout pipe_layout(int dtype, int d, int imax, int omax) {
+__host__ __device__ inline PipeLayout pipe_layout(int dtype, int d, int imax, int omax, int ring) {
   const int eb = dtype == 2 ? 8 : dtype == 1 ? 2 : 4, tb = dtype == 2 ? 8 : 4;
   PipeLayout L;
   L.RS = d * eb + 16;
   L.CS = (omax + 3) & ~3;
-  L.buf = (imax + omax) * L.RS;
-  L.ofp = 2 * L.buf;
+  L.buf = ring * L.RS;
+  L.ofp = L.buf;
   L.coef = L.ofp + omax * d * tb;
   L.slot = L.coef + imax * L.CS * tb;
   L.bytes = (L.slot + 4 * (imax + omax) + 15) & ~15;
@@ -489,16 +495,17 @@ __device__ __forceinline__ int row_id(const int (&id)[3], int r) {  // uniform o
 
 template <int DT, int OMX>
 __global__ void __launch_bounds__(256) adjoint_pipe_kernel(
-    int d, int n, int imax, int omax, const int32_t* in_ptr, const int32_t* in_ids, const int32_t* in_first,
-    const int32_t* out_ptr, const int32_t* out_ids, const int32_t* out_meta, const void* wih, const void* woh,
-    int64_t V, const int32_t* incl_in, const int32_t* incl_out, typename Pipe<DT>::T* g_in,
+    int d, int n, int imax, int omax, int ring, const int32_t* in_ptr, const int32_t* in_ids,
+    const int32_t* in_first, const int32_t* out_ptr, const int32_t* out_ids, const int32_t* out_meta,
+    const void* wih, const void* woh, int64_t V, const int32_t* incl_in, const int32_t* incl_out,
+    typename Pipe<DT>::T* g_in,
     typename Pipe<DT>::T* g_out, double* loss_parts) {
   typedef typename Pipe<DT>::T T;
   constexpr int EB = Pipe<DT>::kBytes;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = lane_id(), wpb = blockDim.x >> 5;
   const int gw = blockIdx.x * wpb + (threadIdx.x >> 5), S = gridDim.x * wpb;
-  const PipeLayout L = pipe_layout(DT, d, imax, omax);
+  const PipeLayout L = pipe_layout(DT, d, imax, omax, ring);
   unsigned char* wbase = smem_raw + (size_t)(threadIdx.x >> 5) * L.bytes;
   T* ofp = reinterpret_cast<T*>(wbase + L.ofp);
   T* coef = reinterpret_cast<T*>(wbase + L.coef);
@@ -559,7 +566,7 @@ __global__ void __launch_bounds__(256) adjoint_pipe_kernel(
     load_slots(cur, idc, slc);
   }
   Extent nxt = load_extent(b + S, n, in_ptr, in_first, out_ptr);
-  int s = 0;
+  int sc = 0;  // ring row of the current minibatch's first row
   T loss = 0;
   const int nq = d >> 2;
   while (b < n) {
@@ -568,7 +575,7 @@ __global__ void __launch_bounds__(256) adjoint_pipe_kernel(
     int idn[3], sln[3] = {0, 0, 0};
     load_ids(nxt, nxt_ok, in_ids, out_ids, idn);
     const Extent nn = load_extent(bn + S, n, in_ptr, in_first, out_ptr);
-    unsigned char* buf = wbase + (size_t)s * L.buf;
+    unsigned char* buf = wbase + (size_t)sc * L.RS;
     cp_async_wait_all();
     if (cur_ok) {
 #pragma unroll
@@ -613,6 +620,7 @@ __global__ void __launch_bounds__(256) adjoint_pipe_kernel(
           float2 fp[OMX];
 #pragma unroll
           for (int i = 0; i < OMX; i++) fp[i] = make_float2(0.f, 0.f);
+#pragma unroll 2
           for (int k = 0; k < d; k += VK) {
             float xv[VK];
             Pipe<DT>::chunk4(xr + k * EB, *reinterpret_cast<float(*)[4]>(xv));
@@ -646,52 +654,100 @@ __global__ void __launch_bounds__(256) adjoint_pipe_kernel(
     }
     // the next minibatch's rows into the other buffer, its slots behind them
     nxt_ok = nxt_ok && ids_ok(nxt, idn);
-    if (nxt_ok) {
-      issue_copies(nxt, idn, wbase + (size_t)(s ^ 1) * L.buf);
+    // the next minibatch's rows go after the current ones, or at the ring's start, when
+    // they fit beside them; otherwise once the current rows are done with
+    const int rc = cur_ok ? cur.I + cur.O : 0, rn = nxt.I + nxt.O;
+    int sn = sc + rc + rn <= ring ? sc + rc : rn <= sc ? 0 : -1;
+    if (nxt_ok && sn >= 0) {
+      issue_copies(nxt, idn, wbase + (size_t)sn * L.RS);
       load_slots(nxt, idn, sln);
     }
     if (cur_ok) {
       // gradient rows, column-parallel: dL/dWih[x_j] = sum_i c_ij Woh[o_i] (order i) and
       // dL/dWoh[o_i] = sum_j c_ij Wih[x_j] (order j)
       for (int q = lane; q < nq; q += 32) {
-        T ov[OMX][4], ao[OMX][4];
+        if constexpr (DT == 2) {
+          T ov[OMX][4], ao[OMX][4];
 #pragma unroll
-        for (int i = 0; i < OMX; i++)
+          for (int i = 0; i < OMX; i++)
 #pragma unroll
-          for (int t = 0; t < 4; t++) ov[i][t] = ao[i][t] = 0;
+            for (int t = 0; t < 4; t++) ov[i][t] = ao[i][t] = 0;
 #pragma unroll
-        for (int i = 0; i < OMX; i++)
-          if (i < O) lds4(ofp + (size_t)i * d + 4 * q, ov[i]);
-        for (int j = 0; j < I; j++) {
-          T xv[4];
-          Pipe<DT>::chunk4(buf + (size_t)j * L.RS + 4 * q * EB, xv);
-          const T* cj = coef + (size_t)j * L.CS;
-          T ai[4] = {0, 0, 0, 0};
+          for (int i = 0; i < OMX; i++)
+            if (i < O) lds4(ofp + (size_t)i * d + 4 * q, ov[i]);
+#pragma unroll 2
+          for (int j = 0; j < I; j++) {
+            T xv[4];
+            Pipe<DT>::chunk4(buf + (size_t)j * L.RS + 4 * q * EB, xv);
+            const T* cj = coef + (size_t)j * L.CS;
+            T ai[4] = {0, 0, 0, 0};
+#pragma unroll
+            for (int i = 0; i < OMX; i++)
+              if (i < O) {
+                const T c = cj[i];
+#pragma unroll
+                for (int t = 0; t < 4; t++) {
+                  ai[t] = fma_t(c, ov[i][t], ai[t]);
+                  ao[i][t] = fma_t(c, xv[t], ao[i][t]);
+                }
+              }
+            atomic_add4(g_in + (size_t)slot[j] * d + 4 * q, ai);
+          }
+#pragma unroll
+          for (int i = 0; i < OMX; i++)
+            if (i < O) atomic_add4(g_out + (size_t)slot[I + i] * d + 4 * q, ao[i]);
+        } else {
+          // packed fp32 pairs: the same fused multiply-adds in the same order
+          float2 ov[OMX][2], ao[OMX][2];
+#pragma unroll
+          for (int i = 0; i < OMX; i++) {
+            ov[i][0] = ov[i][1] = ao[i][0] = ao[i][1] = make_float2(0.f, 0.f);
+            if (i < O) {
+              const float4 o4 = *reinterpret_cast<const float4*>(ofp + (size_t)i * d + 4 * q);
+              ov[i][0] = make_float2(o4.x, o4.y), ov[i][1] = make_float2(o4.z, o4.w);
+            }
+          }
+#pragma unroll 2
+          for (int j = 0; j < I; j++) {
+            float xv[4];
+            Pipe<DT>::chunk4(buf + (size_t)j * L.RS + 4 * q * EB, xv);
+            const float2 x01 = make_float2(xv[0], xv[1]), x23 = make_float2(xv[2], xv[3]);
+            const float* cj = coef + (size_t)j * L.CS;
+            float2 a01 = make_float2(0.f, 0.f), a23 = a01;
+#pragma unroll
+            for (int i = 0; i < OMX; i++)
+              if (i < O) {
+                const float2 c2 = make_float2(cj[i], cj[i]);
+                a01 = __ffma2_rn(c2, ov[i][0], a01);
+                a23 = __ffma2_rn(c2, ov[i][1], a23);
+                ao[i][0] = __ffma2_rn(c2, x01, ao[i][0]);
+                ao[i][1] = __ffma2_rn(c2, x23, ao[i][1]);
+              }
+            const float ai[4] = {a01.x, a01.y, a23.x, a23.y};
+            atomic_add4(g_in + (size_t)slot[j] * d + 4 * q, ai);
+          }
 #pragma unroll
           for (int i = 0; i < OMX; i++)
             if (i < O) {
-              const T c = cj[i];
-#pragma unroll
-              for (int t = 0; t < 4; t++) {
-                ai[t] = fma_t(c, ov[i][t], ai[t]);
-                ao[i][t] = fma_t(c, xv[t], ao[i][t]);
-              }
+              const float v[4] = {ao[i][0].x, ao[i][0].y, ao[i][1].x, ao[i][1].y};
+              atomic_add4(g_out + (size_t)slot[I + i] * d + 4 * q, v);
             }
-          atomic_add4(g_in + (size_t)slot[j] * d + 4 * q, ai);
         }
-#pragma unroll
-        for (int i = 0; i < OMX; i++)
-          if (i < O) atomic_add4(g_out + (size_t)slot[I + i] * d + 4 * q, ao[i]);
       }
     }
     __syncwarp();
+    if (nxt_ok && sn < 0) {
+      sn = 0;
+      issue_copies(nxt, idn, wbase);
+      load_slots(nxt, idn, sln);
+    }
     b = bn;
     cur = nxt;
     nxt = nn;
     cur_ok = nxt_ok;
 #pragma unroll
     for (int m = 0; m < 3; m++) idc[m] = idn[m], slc[m] = sln[m];
-    s ^= 1;
+    sc = sn < 0 ? 0 : sn;
   }
   cp_async_wait_all();
   for (int sh = 16; sh > 0; sh >>= 1) loss += __shfl_xor_sync(kFull, loss, sh);
@@ -753,7 +809,7 @@ cudaError_t launch_adjoint_prepare(int dtype, int d, int n, int64_t V, const int
   if ((e = cudaMemsetAsync(loss, 0, sizeof(double), s)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(loss_parts_of(scratch, V), 0, 256 * sizeof(double), s)) != cudaSuccess) return e;
   if (n > 0)
-    mark_rows_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16), 256, 0, s>>>(
+    mark_rows_kernel<<<(unsigned)std::min<int64_t>(((int64_t)n + 7) / 8, 152 * 16), 256, 0, s>>>(
         n, in_ptr, in_ids, in_first, out_ptr, out_ids, V, incl_in, incl_out, status, status + 1);
   scan_and_emit(incl_in, V, sums_in, grad_in_ids, s);
   scan_and_emit(incl_out, V, sums_out, grad_out_ids, s);
@@ -811,10 +867,20 @@ cudaError_t launch_adjoint(int dtype, int d, int n, int64_t V, int imax, int oma
   const bool v4 = d % 4 == 0;
   // the pipelined kernel when rows are whole 16-byte chunks at 16-byte aligned addresses
   const int eb = dtype == 2 ? 8 : dtype == 1 ? 2 : 4;
-  const PipeLayout PL = pipe_layout(dtype, d, imax, omax);
+  // a ring of one minibatch's rows (see adjoint_pipe_kernel)
+  const int ring = imax + omax;
+  const PipeLayout PL = pipe_layout(dtype, d, imax, omax, ring);
   if (v4 && (d * eb) % 16 == 0 && ((uintptr_t)wih & 15) == 0 && ((uintptr_t)woh & 15) == 0 &&
       PL.bytes <= 232448) {
-    const int pw = std::max(1, std::min(8, 232448 / PL.bytes));
+    // warps per block: the most resident warps per SM (228 KB of shared memory, 1 KB
+    // reserved per block), the larger block on a tie
+    int pw = 1, best = 0;
+    for (int w = 1; w <= 8; w++) {
+      const int per_block = w * PL.bytes + 1024;
+      if (w * PL.bytes > 232448) break;
+      const int warps = (233472 / per_block) * w;
+      if (warps >= best) best = warps, pw = w;
+    }
     const size_t psmem = (size_t)pw * PL.bytes;
     int dev = 0, sms = 0;
     if ((e = cudaGetDevice(&dev)) || (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev))) return e;
@@ -829,7 +895,7 @@ cudaError_t launch_adjoint(int dtype, int d, int n, int64_t V, int imax, int oma
       return e;                                                                                                 \
     const unsigned pb = (unsigned)std::max<int64_t>(                                                            \
         1, std::min<int64_t>((n + pw - 1) / pw, (int64_t)sms * std::max(per_sm, 1)));                           \
-    adjoint_pipe_kernel<DT, OMX><<<pb, 32 * pw, psmem, s>>>(d, n, imax, omax, in_ptr, in_ids, in_first, out_ptr,  \
+    adjoint_pipe_kernel<DT, OMX><<<pb, 32 * pw, psmem, s>>>(d, n, imax, omax, ring, in_ptr, in_ids, in_first, out_ptr, \
                                                             out_ids, out_meta, wih, woh, V, incl_in, incl_out,   \
                                                             static_cast<TT*>(grad_in),                          \
                                                             static_cast<TT*>(grad_out), parts);                 \

@@ -13,13 +13,16 @@
 //   1. each thread summarises its 32 bytes as a Span (outputs it emits, whether its first
 //      significant byte is a newline whose walk end depends on what precedes it, and the
 //      kind of its last significant byte); a block scan gives the tile's Span;
-//   2. one block scans the tile Spans (64-bit output counts);
+//   2. the tile Spans are scanned in two levels (64-bit output counts): groups of 1024
+//      tiles by one block each, the group totals by one block, then the group prefixes
+//      are added to the tiles';
 //   3. each thread rebuilds its exclusive prefix and writes ids and walk ends at their
 //      final offsets; an id is parsed backward from its last digit (at most 10 digits, a
 //      16-byte halo before the tile holds the start of an id cut by the tile edge).
 // Span combination is associative, so the order of the scans does not matter.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "dsgl_device.cuh"
@@ -210,9 +213,9 @@ __global__ void __launch_bounds__(kIngThreads) ingest_count_kernel(const uint8_t
   if (threadIdx.x == 0) tile_span[blockIdx.x] = total;
 }
 
-// Exclusive scan of the tile Spans by one block, 1024 consecutive tiles per round (coalesced
-// reads, block scan, carry to the next round); the text starts as if after a newline.
-// out[t] = prefix of tile t; out[ntiles] = the whole text.
+// Exclusive scan of Spans by one block, 1024 consecutive Spans per round (coalesced reads,
+// block scan, carry to the next round); the text starts as if after a newline.  Used on
+// the group totals: out[g] = prefix of group g; out[ngroups] = the whole text.
 __global__ void __launch_bounds__(kScanBlock) ingest_scan_kernel(const Span* tile_span, int64_t ntiles, Span* out) {
   __shared__ Span warp_tot[kScanBlock / 32];
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
@@ -253,6 +256,51 @@ __global__ void __launch_bounds__(kScanBlock) ingest_scan_kernel(const Span* til
     __syncthreads();
   }
   if (threadIdx.x == 0) out[ntiles] = carry;
+}
+
+// Pass 2, first level: one block per group of kScanBlock consecutive tiles; out[t] = prefix
+// of tile t within its group, group_tot[g] = the group's Span.
+__global__ void __launch_bounds__(kScanBlock) ingest_scan_groups_kernel(const Span* tile_span, int64_t ntiles,
+                                                                       Span* out, Span* group_tot) {
+  __shared__ Span warp_tot[kScanBlock / 32];
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int64_t t = (int64_t)blockIdx.x * kScanBlock + threadIdx.x;
+  const Span v = t < ntiles ? tile_span[t] : span_identity();
+  Span inc = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    Span u;
+    u.cnt = __shfl_up_sync(kFull, inc.cnt, o);
+    u.pend = __shfl_up_sync(kFull, inc.pend, o);
+    u.last = __shfl_up_sync(kFull, inc.last, o);
+    if (lane >= o) inc = span_combine(u, inc);
+  }
+  if (lane == 31) warp_tot[wp] = inc;
+  __syncthreads();
+  if (wp == 0) {
+    Span w = warp_tot[lane];
+    for (int o = 1; o < 32; o <<= 1) {
+      Span u;
+      u.cnt = __shfl_up_sync(kFull, w.cnt, o);
+      u.pend = __shfl_up_sync(kFull, w.pend, o);
+      u.last = __shfl_up_sync(kFull, w.last, o);
+      if (lane >= o) w = span_combine(u, w);
+    }
+    warp_tot[lane] = w;
+  }
+  __syncthreads();
+  Span ex;
+  ex.cnt = __shfl_up_sync(kFull, inc.cnt, 1);
+  ex.pend = __shfl_up_sync(kFull, inc.pend, 1);
+  ex.last = __shfl_up_sync(kFull, inc.last, 1);
+  if (lane == 0) ex = span_identity();
+  if (t < ntiles) out[t] = span_combine(wp > 0 ? warp_tot[wp - 1] : span_identity(), ex);
+  if (threadIdx.x == 0) group_tot[blockIdx.x] = warp_tot[kScanBlock / 32 - 1];
+}
+
+// Pass 2, last step: every tile's prefix behind its group's; out[ntiles] = the whole text.
+__global__ void ingest_scan_add_kernel(Span* out, int64_t ntiles, const Span* group_pre, int64_t ngroups) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t <= ntiles; t += (int64_t)gridDim.x * blockDim.x)
+    out[t] = t < ntiles ? span_combine(group_pre[t / kScanBlock], out[t]) : group_pre[ngroups];
 }
 
 __global__ void __launch_bounds__(kIngThreads) ingest_emit_kernel(const uint8_t* b, int64_t n, bool aligned,
@@ -330,9 +378,11 @@ __global__ void vertex_count_kernel(const int32_t* tokens, int64_t n, int32_t* c
 
 }  // namespace
 
+// scratch: tile Spans, tile prefixes (+ the whole text), the error and largest-id words
+// (64 bytes), then the group totals and group prefixes (+ the whole text)
 size_t ingest_scratch_bytes(int64_t n) {
-  const int64_t ntiles = (n + 1 + kIngTile - 1) / kIngTile;
-  return sizeof(Span) * (size_t)(2 * ntiles + 1) + 64;
+  const int64_t ntiles = (n + 1 + kIngTile - 1) / kIngTile, ngroups = (ntiles + kScanBlock - 1) / kScanBlock;
+  return sizeof(Span) * (size_t)(2 * ntiles + 1) + 64 + sizeof(Span) * (size_t)(2 * ngroups + 1);
 }
 
 cudaError_t launch_ingest_count(const uint8_t* bytes, int64_t n, void* scratch, unsigned long long* n_out,
@@ -347,7 +397,15 @@ cudaError_t launch_ingest_count(const uint8_t* bytes, int64_t n, void* scratch, 
   const bool aligned = (reinterpret_cast<uintptr_t>(bytes) & 15) == 0;
   ingest_count_kernel<<<(unsigned)ntiles, kIngThreads, 0, s>>>(bytes, n, aligned, tile_span, err);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  ingest_scan_kernel<<<1, kScanBlock, 0, s>>>(tile_span, ntiles, prefix);
+  // tile prefixes in two levels: within groups of kScanBlock tiles (one block each), the
+  // group totals by one block, then the group prefixes added to the tiles'
+  const int64_t ngroups = (ntiles + kScanBlock - 1) / kScanBlock;
+  Span* group_tot = reinterpret_cast<Span*>(reinterpret_cast<char*>(prefix + ntiles + 1) + 64);
+  Span* group_pre = group_tot + ngroups;
+  ingest_scan_groups_kernel<<<(unsigned)ngroups, kScanBlock, 0, s>>>(tile_span, ntiles, prefix, group_tot);
+  ingest_scan_kernel<<<1, kScanBlock, 0, s>>>(group_tot, ngroups, group_pre);
+  ingest_scan_add_kernel<<<(unsigned)std::min<int64_t>((ntiles + 256) / 256, 152 * 8), 256, 0, s>>>(
+      prefix, ntiles, group_pre, ngroups);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   Span whole;
   if ((e = cudaMemcpyAsync(&whole, prefix + ntiles, sizeof whole, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||

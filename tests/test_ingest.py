@@ -123,6 +123,28 @@ def test_gpu_parse_matches_oracle(sgns_lib, oracle_mod):
 
 
 @pytest.mark.gpu
+def test_gpu_parse_across_scan_groups(sgns_lib, oracle_mod):
+    """Texts longer than one scan group (1024 tiles of 8 KB), so the tile prefixes come from
+    the two-level scan: ordinary walks over several groups, whole groups of blanks or
+    newlines, a walk that spans them and ids cut by a group edge."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(5)
+    block = random_text(rng, 20000) + b"\n"
+    group = 1024 * 8192
+    texts = [block * 7,
+             block + b" " * (group + 100) + b" 77 78" + b" " * group + b"\n 79\n" + block,
+             b"\n" * (2 * group + 5) + b" 1 2 3"]
+    for shift in (0, 1, 5):
+        texts.append(b" " * (group - shift) + b"1234567 42\n 9")
+    for text in texts:
+        c, ref, mx, _ = oracle_mod.parse_walks(text)
+        assert c == 0
+        out, gmx = _gpu_parse(text, torch)
+        assert np.array_equal(out, ref), (len(text), len(out), len(ref))
+        assert gmx == mx
+
+
+@pytest.mark.gpu
 def test_gpu_parse_errors(sgns_lib, oracle_mod):
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(12)
