@@ -62,6 +62,9 @@ __device__ __forceinline__ uint8_t text_byte(const uint8_t* b, int64_t n, int64_
   return i < n ? __ldg(b + i) : (i == n ? (uint8_t)'\n' : (uint8_t)' ');
 }
 
+__device__ __constant__ uint32_t kPow10[9] = {1u, 10u, 100u, 1000u, 10000u, 100000u, 1000000u, 10000000u,
+                                              100000000u};
+
 constexpr int kStageChunks = (kIngHalo + kIngTile + 16) / 16;  // 16-byte chunks staged per tile
 
 // Stages tile bytes [base - halo, base + kIngTile + 16) in shared memory: 16 bytes per load
@@ -151,6 +154,16 @@ __device__ __forceinline__ Emits emits(const Masks& m, bool next_digit, uint32_t
   return e;
 }
 
+// Span of one thread's 32 bytes from its masks and its outputs with no carry.
+__device__ __forceinline__ Span span_of(const Masks& m, const Emits& e, uint32_t pend) {
+  const uint32_t sig = m.dig | m.nl;
+  Span sp;
+  sp.cnt = __popc(e.ids) + __popc(e.walks);
+  sp.pend = pend;
+  sp.last = sig == 0 ? SIG_NONE : (((m.dig >> (31 - __clz(sig))) & 1u) ? SIG_DIGIT : SIG_NL);
+  return sp;
+}
+
 // Span of one thread's 32 bytes; s points at the thread's first byte in shared memory.
 template <bool kCheck>
 __device__ __forceinline__ Span thread_span(const uint8_t* s, int64_t first, int64_t* bad) {
@@ -158,12 +171,7 @@ __device__ __forceinline__ Span thread_span(const uint8_t* s, int64_t first, int
   if (m.bad) *bad = first + __ffs(m.bad) - 1;
   uint32_t pend;
   const Emits e = emits(m, is_digit(s[kIngBytes]), SIG_NONE, &pend);
-  const uint32_t sig = m.dig | m.nl;
-  Span sp;
-  sp.cnt = __popc(e.ids) + __popc(e.walks);
-  sp.pend = pend;
-  sp.last = sig == 0 ? SIG_NONE : (((m.dig >> (31 - __clz(sig))) & 1u) ? SIG_DIGIT : SIG_NL);
-  return sp;
+  return span_of(m, e, pend);
 }
 
 // Block-wide exclusive scan of Spans (blockDim.x == kIngThreads); returns the thread's
@@ -313,16 +321,23 @@ __global__ void __launch_bounds__(kIngThreads) ingest_emit_kernel(const uint8_t*
   const int64_t first = base + (int64_t)threadIdx.x * kIngBytes;
   const uint8_t* my = s + kIngHalo + threadIdx.x * kIngBytes;
   int64_t bad = -1;
-  // the count pass has checked every byte; this pass only reads valid text
-  const Span v = first <= n ? thread_span<false>(my, first, &bad) : span_identity();
+  // the count pass has checked every byte; this pass only reads valid text.  The bytes are
+  // classified once: the outputs with no carry give the thread's Span, and once the
+  // prefix is known a pending first newline becomes a walk end when a digit precedes it.
+  Masks m{0u, 0u, 0u};
+  Emits e{0u, 0u};
+  uint32_t pend = 0;
+  if (first <= n) {
+    m = classify<false>(my);
+    e = emits(m, is_digit(my[kIngBytes]), SIG_NONE, &pend);
+  }
+  const Span v = first <= n ? span_of(m, e, pend) : span_identity();
   Span total;
   const Span ex = span_combine(tile_prefix[blockIdx.x], block_exclusive(v, &total));
   long long mx = -1;
   if (first <= n) {
     unsigned long long pos = ex.cnt;
-    const Masks m = classify<false>(my);
-    uint32_t pend;
-    const Emits e = emits(m, is_digit(my[kIngBytes]), ex.last, &pend);
+    if (pend && ex.last == SIG_DIGIT) e.walks |= 1u << (__ffs(m.nl) - 1);
     uint32_t out = e.ids | e.walks;
     while (out) {  // outputs in text order
       const int j = __ffs(out) - 1;
@@ -331,20 +346,28 @@ __global__ void __launch_bounds__(kIngThreads) ingest_emit_kernel(const uint8_t*
         tokens[pos++] = -1;
         continue;
       }
-      // the id ending at byte j, read backward: its last nine digits in 32 bits, then a
-      // tenth (an eleventh digit, or a ten-digit value above 2^31 - 1, is an error)
-      uint32_t low = 0, scale = 1;
-      int k = j, nd = 0;
-      while (nd < 9 && is_digit(my[k])) {
-        low += (uint32_t)(my[k] - '0') * scale;
-        scale *= 10u;
-        nd++;
-        k--;
+      // the id ending at byte j: its length from the digit mask when it starts inside this
+      // thread's bytes, else by reading back over the bytes before them (at most eleven);
+      // its last nine digits are loaded at once and summed in 32 bits, then a tenth (an
+      // eleventh digit, or a ten-digit value above 2^31 - 1, is an error)
+      const uint32_t nondig = ~m.dig & ((1u << j) - 1u);
+      int L;
+      if (nondig) {
+        L = j - (31 - __clz(nondig));
+      } else {
+        L = j + 1;
+        while (L < 11 && is_digit(my[j - L])) L++;
+      }
+      uint32_t low = 0;
+#pragma unroll
+      for (int t = 0; t < 9; t++) {
+        const uint32_t dgt = (uint32_t)(my[j - t] - '0');  // bytes down to my[-8]: halo or earlier threads
+        low += t < L ? dgt * kPow10[t] : 0u;
       }
       uint32_t val = low;
-      if (nd == 9 && is_digit(my[k])) {
-        const uint32_t top = (uint32_t)(my[k] - '0');
-        if (is_digit(my[k - 1]) || top > 2u || (top == 2u && low > 147483647u)) {
+      if (L >= 10) {
+        const uint32_t top = (uint32_t)(my[j - 9] - '0');
+        if (L > 10 || top > 2u || (top == 2u && low > 147483647u)) {
           if (bad < 0) bad = first + j;
           val = 0;
         } else {

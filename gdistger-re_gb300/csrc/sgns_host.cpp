@@ -750,6 +750,11 @@ int32_t sgns_internal_write_embedding(const uint32_t* order, const float* w, int
 // The walker's x * log2(x) table as sgns_info_walks uploads it; exported for the CPU tests.
 void sgns_internal_xlog2x_table(int32_t n, double* t) { xlog2x_table(n, t); }
 
+// The stochastic-rounding bits of the kernels' write-backs (host copy of sr_bits4).
+void sgns_internal_sr_bits4(int64_t n, const uint64_t* ev, const uint32_t* row, const uint32_t* col4, uint64_t* bits) {
+  for (int64_t i = 0; i < n; i++) bits[i] = sr_bits4(ev[i], row[i], col4[i]);
+}
+
 void sgns_default_options(sgns_options* o) {
   std::memset(o, 0, sizeof *o);
   o->size = 100;  // dsgl.hpp:70

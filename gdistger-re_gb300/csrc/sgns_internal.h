@@ -107,10 +107,12 @@ SGNS_HD uint64_t sr_event_key(uint64_t seed, int kind, uint32_t worker, uint64_t
 // event key ev (one SplitMix64 output per write event):
 //   h  = fmix32(lo32(ev) ^ (row * 0x9E3779B1 + col4 * 0x85EBCA77))   (murmur3's 32-bit
 //        finaliser, Appleby 2011; constants of Wellons' low-bias variant),
-//   h2 = high 32 bits of the 64-bit product (h ^ hi32(ev)) * 0xCC9E2D51,
+//   t  = (h ^ hi32(ev)) * 0x9E3779B1 (mod 2^32),  h2 = t ^ (t >> 16),
 //   bits = h2 << 32 | h  (columns 4q, 4q+1 take h; 4q+2, 4q+3 take h2).
-// About a third of the instructions of a 64-bit finaliser per chunk, on the write-back
-// path of every output row of every step.
+// Both words are bijections of uniform words, so every 16-bit field is uniform and the
+// rounding unbiased (the high word of a product by a 32-bit constant would not be: its
+// range ends at the constant).  About half the instructions of a 64-bit finaliser per
+// chunk, on the write-back path of every output row of every step.
 SGNS_HD uint32_t fmix32(uint32_t h) {
   h ^= h >> 16;
   h *= 0x7FEB352Du;
@@ -120,8 +122,8 @@ SGNS_HD uint32_t fmix32(uint32_t h) {
 }
 SGNS_HD uint64_t sr_bits4(uint64_t ev, uint32_t row, uint32_t col4) {
   const uint32_t h = fmix32((uint32_t)ev ^ (row * 0x9E3779B1u + col4 * 0x85EBCA77u));
-  const uint32_t h2 = (uint32_t)(((uint64_t)(h ^ (uint32_t)(ev >> 32)) * 0xCC9E2D51u) >> 32);
-  return ((uint64_t)h2 << 32) | h;
+  const uint32_t t = (h ^ (uint32_t)(ev >> 32)) * 0x9E3779B1u;
+  return ((uint64_t)(t ^ (t >> 16)) << 32) | h;
 }
 SGNS_HD float bf16_bits_to_f32(uint16_t b) {
   uint32_t u = (uint32_t)b << 16;
@@ -274,6 +276,10 @@ extern "C" int32_t sgns_internal_write_embedding(const uint32_t* order, const fl
 // The walker's x * log2(x) table (n entries) exactly as sgns_info_walks builds it; exported
 // for the CPU tests.
 extern "C" void sgns_internal_xlog2x_table(int32_t n, double* t);
+// The stochastic-rounding bits of n (event key, row, column chunk) triples, computed by the
+// host copy of sr_bits4 (the kernels' function); exported for the CPU tests.
+extern "C" void sgns_internal_sr_bits4(int64_t n, const uint64_t* ev, const uint32_t* row, const uint32_t* col4,
+                                       uint64_t* bits);
 // The row draw of sgns_sync_rows from count-sorted counts (no device); exported for the CPU
 // tests.  Returns SGNS_EINVAL (with *n_rows set) when cap is too small.
 extern "C" int32_t sgns_internal_sync_rows(const int32_t* cn_sorted, int64_t V, uint64_t seed, uint64_t round,

@@ -119,6 +119,8 @@ def lib():
         L.sgns_internal_sync_rows.restype = i32
         L.sgns_internal_xlog2x_table.argtypes = [i32, vp]
         L.sgns_internal_xlog2x_table.restype = None
+        L.sgns_internal_sr_bits4.argtypes = [i64, vp, vp, vp, vp]
+        L.sgns_internal_sr_bits4.restype = None
         for name in header_functions():  # every declared entry point must be exported
             getattr(L, name)
         _lib = L
@@ -435,3 +437,14 @@ def xlog2x_table(n):
     t = np.zeros(n, np.float64)
     lib().sgns_internal_xlog2x_table(n, _ptr(t))
     return t
+
+
+def sr_bits4(ev, row, col4):
+    """The stochastic-rounding bits (uint64 per triple) the kernels draw for column chunk
+    col4 of row `row` under event key ev (host copy of the device function, no device)."""
+    ev = np.ascontiguousarray(ev, np.uint64)
+    row = np.ascontiguousarray(row, np.uint32)
+    col4 = np.ascontiguousarray(col4, np.uint32)
+    out = np.zeros(len(ev), np.uint64)
+    lib().sgns_internal_sr_bits4(len(ev), _ptr(ev), _ptr(row), _ptr(col4), _ptr(out))
+    return out

@@ -66,8 +66,8 @@ inline uint64_t sr_event_key(uint64_t seed, int kind, uint32_t worker, uint64_t 
 }
 // 16 random bits for one column: columns 4q, 4q+1 take the low and high halves of
 // h = fmix32(lo32(ev) ^ (row * 0x9E3779B1 + q * 0x85EBCA77)) (murmur3's 32-bit finaliser
-// with Wellons' low-bias constants), columns 4q+2, 4q+3 those of
-// h2 = hi32((h ^ hi32(ev)) * 0xCC9E2D51)
+// with Wellons' low-bias constants), columns 4q+2, 4q+3 those of h2 = t ^ (t >> 16),
+// t = (h ^ hi32(ev)) * 0x9E3779B1 mod 2^32
 inline uint32_t fmix32(uint32_t h) {
   h ^= h >> 16;
   h *= 0x7FEB352Du;
@@ -78,8 +78,8 @@ inline uint32_t fmix32(uint32_t h) {
 inline uint32_t sr_bits16(uint64_t ev, uint32_t row, int col) {
   const uint32_t q = (uint32_t)(col >> 2);
   const uint32_t h = fmix32((uint32_t)ev ^ (row * 0x9E3779B1u + q * 0x85EBCA77u));
-  const uint32_t h2 = (uint32_t)(((uint64_t)(h ^ (uint32_t)(ev >> 32)) * 0xCC9E2D51u) >> 32);
-  const uint64_t bits = ((uint64_t)h2 << 32) | h;
+  const uint32_t t = (h ^ (uint32_t)(ev >> 32)) * 0x9E3779B1u;
+  const uint64_t bits = ((uint64_t)(t ^ (t >> 16)) << 32) | h;
   return (uint32_t)(bits >> ((col & 3) * 16)) & 0xFFFFu;
 }
 inline float bf16_to_f32(uint16_t b) {

@@ -108,10 +108,10 @@ def fmix32(h):
 
 def sr_bits4(key, r, q):
     """64 bits for columns 4q..4q+3 of row r: h = fmix32(lo32(key) ^ (r * 0x9E3779B1 +
-    q * 0x85EBCA77)), h2 = hi32((h ^ hi32(key)) * 0xCC9E2D51), bits = h2 << 32 | h."""
+    q * 0x85EBCA77)), t = (h ^ hi32(key)) * 0x9E3779B1 mod 2^32, bits = (t ^ t >> 16) << 32 | h."""
     h = fmix32((key & M32) ^ ((r * 0x9E3779B1 + q * 0x85EBCA77) & M32))
-    h2 = ((h ^ (key >> 32)) * 0xCC9E2D51) >> 32
-    return (h2 << 32) | h
+    t = ((h ^ (key >> 32)) * 0x9E3779B1) & M32
+    return ((t ^ (t >> 16)) << 32) | h
 
 
 def sr_rows(v, seed, kind, b):
