@@ -451,14 +451,14 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 struct PipeLayout {
   int RS, CS, buf, ofp, coef, slot, bytes;
 };
-__host__ __device__ inline PipeLayout pipe_layout(int dtype, int d, int imax, int omax, int ring) {
+__host__ __device__ inline PipeLayout pipe_layout(int dtype, int d, int imax, int omax, int omx, int ring) {
   const int eb = dtype == 2 ? 8 : dtype == 1 ? 2 : 4, tb = dtype == 2 ? 8 : 4;
   PipeLayout L;
   L.RS = d * eb + 16;
-  L.CS = (omax + 3) & ~3;
+  L.CS = (omx + 3) & ~3;
   L.buf = ring * L.RS;
   L.ofp = L.buf;
-  L.coef = L.ofp + omax * d * tb;
+  L.coef = L.ofp + omx * d * tb;
   L.slot = L.coef + imax * L.CS * tb;
   L.bytes = (L.slot + 4 * (imax + omax) + 15) & ~15;
   return L;
@@ -505,7 +505,7 @@ __global__ void __launch_bounds__(256) adjoint_pipe_kernel(
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = lane_id(), wpb = blockDim.x >> 5;
   const int gw = blockIdx.x * wpb + (threadIdx.x >> 5), S = gridDim.x * wpb;
-  const PipeLayout L = pipe_layout(DT, d, imax, omax, ring);
+  const PipeLayout L = pipe_layout(DT, d, imax, omax, OMX, ring);
   unsigned char* wbase = smem_raw + (size_t)(threadIdx.x >> 5) * L.bytes;
   T* ofp = reinterpret_cast<T*>(wbase + L.ofp);
   T* coef = reinterpret_cast<T*>(wbase + L.coef);
@@ -585,11 +585,12 @@ __global__ void __launch_bounds__(256) adjoint_pipe_kernel(
     __syncwarp();
     const int I = cur.I, O = cur.O;
     if (cur_ok) {
-      // widen the output rows once (column-parallel)
-      for (int i = 0; i < O; i++)
+      // widen the output rows once (column-parallel); rows O .. OMX-1 are zero, so the
+      // products below run over the kernel's full output capacity without tests
+      for (int i = 0; i < OMX; i++)
         for (int q = lane; q < nq; q += 32) {
-          T v[4];
-          Pipe<DT>::chunk4(buf + (size_t)(I + i) * L.RS + 4 * q * EB, v);
+          T v[4] = {0, 0, 0, 0};
+          if (i < O) Pipe<DT>::chunk4(buf + (size_t)(I + i) * L.RS + 4 * q * EB, v);
           sts4(ofp + (size_t)i * d + 4 * q, v);
         }
       __syncwarp();
@@ -605,13 +606,12 @@ __global__ void __launch_bounds__(256) adjoint_pipe_kernel(
             T xv[4];
             Pipe<DT>::chunk4(xr + k * EB, xv);
 #pragma unroll
-            for (int i = 0; i < OMX; i++)
-              if (i < O) {
-                T ov[4];
-                lds4(ofp + (size_t)i * d + k, ov);
+            for (int i = 0; i < OMX; i++) {
+              T ov[4];
+              lds4(ofp + (size_t)i * d + k, ov);
 #pragma unroll
-                for (int t = 0; t < 4; t++) f[i] = fma_t(ov[t], xv[t], f[i]);
-              }
+              for (int t = 0; t < 4; t++) f[i] = fma_t(ov[t], xv[t], f[i]);
+            }
           }
         } else {
           // 16 bytes of the input row per step: 8 bf16 or 4 fp32 elements, even and odd
@@ -626,28 +626,28 @@ __global__ void __launch_bounds__(256) adjoint_pipe_kernel(
             Pipe<DT>::chunk4(xr + k * EB, *reinterpret_cast<float(*)[4]>(xv));
             if constexpr (VK == 8) Pipe<DT>::chunk4(xr + k * EB + 8, *reinterpret_cast<float(*)[4]>(xv + 4));
 #pragma unroll
-            for (int i = 0; i < OMX; i++)
-              if (i < O) {
+            for (int i = 0; i < OMX; i++) {
 #pragma unroll
-                for (int h = 0; h < VK; h += 4) {
-                  const float4 o4 = *reinterpret_cast<const float4*>(ofp + (size_t)i * d + k + h);
-                  fp[i] = __ffma2_rn(make_float2(o4.x, o4.y), make_float2(xv[h], xv[h + 1]), fp[i]);
-                  fp[i] = __ffma2_rn(make_float2(o4.z, o4.w), make_float2(xv[h + 2], xv[h + 3]), fp[i]);
-                }
+              for (int h = 0; h < VK; h += 4) {
+                const float4 o4 = *reinterpret_cast<const float4*>(ofp + (size_t)i * d + k + h);
+                fp[i] = __ffma2_rn(make_float2(o4.x, o4.y), make_float2(xv[h], xv[h + 1]), fp[i]);
+                fp[i] = __ffma2_rn(make_float2(o4.z, o4.w), make_float2(xv[h + 2], xv[h + 3]), fp[i]);
               }
+            }
           }
 #pragma unroll
           for (int i = 0; i < OMX; i++) f[i] = __fadd_rn(fp[i].x, fp[i].y);
         }
         if (j < I) {
 #pragma unroll
-          for (int i = 0; i < OMX; i++)
+          for (int i = 0; i < OMX; i++) {
+            T c = 0;
             if (i < O) {
               const int label = j < cur.first ? (i == 0) : (i == O - 1);
-              T c;
               pair_terms(f[i], label, (T)out_meta[cur.o0 + i], loss, c);
-              coef[(size_t)j * L.CS + i] = c;
             }
+            coef[(size_t)j * L.CS + i] = c;  // zero past O: those products add nothing
+          }
         }
       }
       __syncwarp();
@@ -673,8 +673,7 @@ __global__ void __launch_bounds__(256) adjoint_pipe_kernel(
 #pragma unroll
             for (int t = 0; t < 4; t++) ov[i][t] = ao[i][t] = 0;
 #pragma unroll
-          for (int i = 0; i < OMX; i++)
-            if (i < O) lds4(ofp + (size_t)i * d + 4 * q, ov[i]);
+          for (int i = 0; i < OMX; i++) lds4(ofp + (size_t)i * d + 4 * q, ov[i]);
 #pragma unroll 2
           for (int j = 0; j < I; j++) {
             T xv[4];
@@ -682,15 +681,14 @@ __global__ void __launch_bounds__(256) adjoint_pipe_kernel(
             const T* cj = coef + (size_t)j * L.CS;
             T ai[4] = {0, 0, 0, 0};
 #pragma unroll
-            for (int i = 0; i < OMX; i++)
-              if (i < O) {
-                const T c = cj[i];
+            for (int i = 0; i < OMX; i++) {
+              const T c = cj[i];
 #pragma unroll
-                for (int t = 0; t < 4; t++) {
-                  ai[t] = fma_t(c, ov[i][t], ai[t]);
-                  ao[i][t] = fma_t(c, xv[t], ao[i][t]);
-                }
+              for (int t = 0; t < 4; t++) {
+                ai[t] = fma_t(c, ov[i][t], ai[t]);
+                ao[i][t] = fma_t(c, xv[t], ao[i][t]);
               }
+            }
             atomic_add4(g_in + (size_t)slot[j] * d + 4 * q, ai);
           }
 #pragma unroll
@@ -701,11 +699,9 @@ __global__ void __launch_bounds__(256) adjoint_pipe_kernel(
           float2 ov[OMX][2], ao[OMX][2];
 #pragma unroll
           for (int i = 0; i < OMX; i++) {
-            ov[i][0] = ov[i][1] = ao[i][0] = ao[i][1] = make_float2(0.f, 0.f);
-            if (i < O) {
-              const float4 o4 = *reinterpret_cast<const float4*>(ofp + (size_t)i * d + 4 * q);
-              ov[i][0] = make_float2(o4.x, o4.y), ov[i][1] = make_float2(o4.z, o4.w);
-            }
+            const float4 o4 = *reinterpret_cast<const float4*>(ofp + (size_t)i * d + 4 * q);
+            ov[i][0] = make_float2(o4.x, o4.y), ov[i][1] = make_float2(o4.z, o4.w);
+            ao[i][0] = ao[i][1] = make_float2(0.f, 0.f);
           }
 #pragma unroll 2
           for (int j = 0; j < I; j++) {
@@ -715,14 +711,13 @@ __global__ void __launch_bounds__(256) adjoint_pipe_kernel(
             const float* cj = coef + (size_t)j * L.CS;
             float2 a01 = make_float2(0.f, 0.f), a23 = a01;
 #pragma unroll
-            for (int i = 0; i < OMX; i++)
-              if (i < O) {
-                const float2 c2 = make_float2(cj[i], cj[i]);
-                a01 = __ffma2_rn(c2, ov[i][0], a01);
-                a23 = __ffma2_rn(c2, ov[i][1], a23);
-                ao[i][0] = __ffma2_rn(c2, x01, ao[i][0]);
-                ao[i][1] = __ffma2_rn(c2, x23, ao[i][1]);
-              }
+            for (int i = 0; i < OMX; i++) {
+              const float2 c2 = make_float2(cj[i], cj[i]);
+              a01 = __ffma2_rn(c2, ov[i][0], a01);
+              a23 = __ffma2_rn(c2, ov[i][1], a23);
+              ao[i][0] = __ffma2_rn(c2, x01, ao[i][0]);
+              ao[i][1] = __ffma2_rn(c2, x23, ao[i][1]);
+            }
             const float ai[4] = {a01.x, a01.y, a23.x, a23.y};
             atomic_add4(g_in + (size_t)slot[j] * d + 4 * q, ai);
           }
@@ -869,7 +864,7 @@ cudaError_t launch_adjoint(int dtype, int d, int n, int64_t V, int imax, int oma
   const int eb = dtype == 2 ? 8 : dtype == 1 ? 2 : 4;
   // a ring of one minibatch's rows (see adjoint_pipe_kernel)
   const int ring = imax + omax;
-  const PipeLayout PL = pipe_layout(dtype, d, imax, omax, ring);
+  const PipeLayout PL = pipe_layout(dtype, d, imax, omax, omax <= 7 ? 7 : kOMax, ring);
   if (v4 && (d * eb) % 16 == 0 && ((uintptr_t)wih & 15) == 0 && ((uintptr_t)woh & 15) == 0 &&
       PL.bytes <= 232448) {
     // warps per block: the most resident warps per SM (228 KB of shared memory, 1 KB
