@@ -493,6 +493,86 @@ __device__ __forceinline__ int row_id(const int (&id)[3], int r) {  // uniform o
   return r < 32 ? a : r < 64 ? b : c;
 }
 
+// f = Out x X^T for one minibatch on the tensor cores (bf16 tables): A = the output rows
+// (16 x 16 per MMA, rows past O zero), B = the input rows (8 inputs x 16 columns per MMA,
+// "col" layout = each input row contiguous), both read as bf16 pairs straight from the
+// ring (row stride RS = 2d + 16 bytes: the 32 lanes' words fall in 32 banks).  The
+// products of bf16 values are exact in fp32 and the sums run in fp32, as in the lane-per-
+// input form (in another order).  Thread (g = lane / 4, t = lane % 4) ends with f for
+// outputs g and g + 8 and inputs 8n + 2t, 8n + 2t + 1 of tile n; it computes those pairs'
+// loss terms and coefficients, so all 32 lanes work on them.  Coefficients of outputs
+// O .. OMX-1 are zero (the backward runs over OMX outputs).
+__device__ __forceinline__ void mma_bf16_16816(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                               uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+__device__ __forceinline__ uint32_t lds_u32(const unsigned char* p) { return *reinterpret_cast<const uint32_t*>(p); }
+
+template <int OMX>
+__device__ __forceinline__ void forward_mma_bf16(const unsigned char* buf, int RS, int d, int I, int O, int first,
+                                                 const int32_t* meta, float* coef, int CS, float& loss) {
+  static_assert(OMX <= 16, "one MMA row block holds the outputs");
+  const int lane = lane_id(), g = lane >> 2, t = lane & 3;
+  for (int e = lane; e < I * OMX; e += 32) {  // zero coefficients past O
+    const int j = e / OMX, i = e - j * OMX;
+    if (i >= O) coef[(size_t)j * CS + i] = 0.f;
+  }
+  const float meta0 = g < O ? (float)meta[g] : 0.f, meta1 = g + 8 < O ? (float)meta[g + 8] : 0.f;
+  const unsigned char* arow0 = buf + (size_t)(I + (g < O ? g : 0)) * RS + 4 * t;
+  const unsigned char* arow1 = buf + (size_t)(I + (g + 8 < O ? g + 8 : 0)) * RS + 4 * t;
+  const int ntiles = (I + 7) >> 3;
+  for (int n0 = 0; n0 < ntiles; n0 += 4) {  // up to four tiles (32 inputs) per round
+    float acc[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+#pragma unroll
+      for (int r = 0; r < 4; r++) acc[u][r] = 0.f;
+    const unsigned char* brow[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int j = (n0 + u) * 8 + g;
+      brow[u] = buf + (size_t)(j < I ? j : 0) * RS + 4 * t;
+    }
+    for (int k0 = 0; k0 < d; k0 += 16) {
+      const int kb = 2 * k0;            // byte offset of column k0
+      const bool hi = k0 + 8 < d;       // columns k0+8 .. k0+15 exist (d % 8 == 0)
+      const uint32_t a0 = g < O ? lds_u32(arow0 + kb) : 0u;
+      const uint32_t a2 = g < O && hi ? lds_u32(arow0 + kb + 16) : 0u;
+      const uint32_t a1 = OMX > 8 && g + 8 < O ? lds_u32(arow1 + kb) : 0u;
+      const uint32_t a3 = OMX > 8 && g + 8 < O && hi ? lds_u32(arow1 + kb + 16) : 0u;
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        if (n0 + u < ntiles) {  // uniform
+          const uint32_t b0 = lds_u32(brow[u] + kb), b1 = hi ? lds_u32(brow[u] + kb + 16) : 0u;
+          mma_bf16_16816(acc[u], a0, a1, a2, a3, b0, b1);
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int i = g + 8 * h;
+        if ((h == 1 && OMX <= 8) || i >= O) continue;
+#pragma unroll
+        for (int e = 0; e < 2; e++) {
+          const int j = (n0 + u) * 8 + 2 * t + e;
+          if (j < I) {
+            const int label = j < first ? (i == 0) : (i == O - 1);
+            float c;
+            pair_terms(acc[u][2 * h + e], label, h ? meta1 : meta0, loss, c);
+            coef[(size_t)j * CS + i] = c;
+          }
+        }
+      }
+    }
+  }
+}
+
 template <int DT, int OMX>
 __global__ void __launch_bounds__(256) adjoint_pipe_kernel(
     int d, int n, int imax, int omax, int ring, const int32_t* in_ptr, const int32_t* in_ids,
@@ -594,59 +674,63 @@ __global__ void __launch_bounds__(256) adjoint_pipe_kernel(
           sts4(ofp + (size_t)i * d + 4 * q, v);
         }
       __syncwarp();
-      // dot products, one lane per input
-      for (int j0 = 0; j0 < I; j0 += 32) {
-        const int j = j0 + lane;
-        const unsigned char* xr = buf + (size_t)(j < I ? j : 0) * L.RS;
-        T f[OMX];
-        if constexpr (DT == 2) {
-#pragma unroll
-          for (int i = 0; i < OMX; i++) f[i] = 0;
-          for (int k = 0; k < d; k += 4) {
-            T xv[4];
-            Pipe<DT>::chunk4(xr + k * EB, xv);
-#pragma unroll
-            for (int i = 0; i < OMX; i++) {
-              T ov[4];
-              lds4(ofp + (size_t)i * d + k, ov);
-#pragma unroll
-              for (int t = 0; t < 4; t++) f[i] = fma_t(ov[t], xv[t], f[i]);
-            }
-          }
-        } else {
-          // 16 bytes of the input row per step: 8 bf16 or 4 fp32 elements, even and odd
-          // partial sums in packed fp32 pairs
-          constexpr int VK = 16 / EB;
-          float2 fp[OMX];
-#pragma unroll
-          for (int i = 0; i < OMX; i++) fp[i] = make_float2(0.f, 0.f);
-#pragma unroll 2
-          for (int k = 0; k < d; k += VK) {
-            float xv[VK];
-            Pipe<DT>::chunk4(xr + k * EB, *reinterpret_cast<float(*)[4]>(xv));
-            if constexpr (VK == 8) Pipe<DT>::chunk4(xr + k * EB + 8, *reinterpret_cast<float(*)[4]>(xv + 4));
-#pragma unroll
-            for (int i = 0; i < OMX; i++) {
-#pragma unroll
-              for (int h = 0; h < VK; h += 4) {
-                const float4 o4 = *reinterpret_cast<const float4*>(ofp + (size_t)i * d + k + h);
-                fp[i] = __ffma2_rn(make_float2(o4.x, o4.y), make_float2(xv[h], xv[h + 1]), fp[i]);
-                fp[i] = __ffma2_rn(make_float2(o4.z, o4.w), make_float2(xv[h + 2], xv[h + 3]), fp[i]);
+      if constexpr (DT == 1) {
+        forward_mma_bf16<OMX>(buf, L.RS, d, I, O, cur.first, out_meta + cur.o0, coef, L.CS, loss);
+      } else {
+        // dot products, one lane per input
+        for (int j0 = 0; j0 < I; j0 += 32) {
+          const int j = j0 + lane;
+          const unsigned char* xr = buf + (size_t)(j < I ? j : 0) * L.RS;
+          T f[OMX];
+          if constexpr (DT == 2) {
+  #pragma unroll
+            for (int i = 0; i < OMX; i++) f[i] = 0;
+            for (int k = 0; k < d; k += 4) {
+              T xv[4];
+              Pipe<DT>::chunk4(xr + k * EB, xv);
+  #pragma unroll
+              for (int i = 0; i < OMX; i++) {
+                T ov[4];
+                lds4(ofp + (size_t)i * d + k, ov);
+  #pragma unroll
+                for (int t = 0; t < 4; t++) f[i] = fma_t(ov[t], xv[t], f[i]);
               }
             }
-          }
-#pragma unroll
-          for (int i = 0; i < OMX; i++) f[i] = __fadd_rn(fp[i].x, fp[i].y);
-        }
-        if (j < I) {
-#pragma unroll
-          for (int i = 0; i < OMX; i++) {
-            T c = 0;
-            if (i < O) {
-              const int label = j < cur.first ? (i == 0) : (i == O - 1);
-              pair_terms(f[i], label, (T)out_meta[cur.o0 + i], loss, c);
+          } else {
+            // 16 bytes of the input row per step: 8 bf16 or 4 fp32 elements, even and odd
+            // partial sums in packed fp32 pairs
+            constexpr int VK = 16 / EB;
+            float2 fp[OMX];
+  #pragma unroll
+            for (int i = 0; i < OMX; i++) fp[i] = make_float2(0.f, 0.f);
+  #pragma unroll 2
+            for (int k = 0; k < d; k += VK) {
+              float xv[VK];
+              Pipe<DT>::chunk4(xr + k * EB, *reinterpret_cast<float(*)[4]>(xv));
+              if constexpr (VK == 8) Pipe<DT>::chunk4(xr + k * EB + 8, *reinterpret_cast<float(*)[4]>(xv + 4));
+  #pragma unroll
+              for (int i = 0; i < OMX; i++) {
+  #pragma unroll
+                for (int h = 0; h < VK; h += 4) {
+                  const float4 o4 = *reinterpret_cast<const float4*>(ofp + (size_t)i * d + k + h);
+                  fp[i] = __ffma2_rn(make_float2(o4.x, o4.y), make_float2(xv[h], xv[h + 1]), fp[i]);
+                  fp[i] = __ffma2_rn(make_float2(o4.z, o4.w), make_float2(xv[h + 2], xv[h + 3]), fp[i]);
+                }
+              }
             }
-            coef[(size_t)j * L.CS + i] = c;  // zero past O: those products add nothing
+  #pragma unroll
+            for (int i = 0; i < OMX; i++) f[i] = __fadd_rn(fp[i].x, fp[i].y);
+          }
+          if (j < I) {
+  #pragma unroll
+            for (int i = 0; i < OMX; i++) {
+              T c = 0;
+              if (i < O) {
+                const int label = j < cur.first ? (i == 0) : (i == O - 1);
+                pair_terms(f[i], label, (T)out_meta[cur.o0 + i], loss, c);
+              }
+              coef[(size_t)j * L.CS + i] = c;  // zero past O: those products add nothing
+            }
           }
         }
       }
