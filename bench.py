@@ -907,13 +907,17 @@ def main():
         except Exception as e:
             line["minibatch_error"] = {"error": "%s: %s" % (type(e).__name__, e)}
     if not args.skip_extras:
-        # e2e through the reference-facing call, host buffers in, statistics out
-        # one untimed call first: the first GPU read of a pinned buffer sets up its host-page
-        # translations (about 0.2 s for 3.2 GB); a caller that reuses the buffer pays it once
-        # the trained input table comes back too, as the reference's my_saveModel reads it
+        # e2e through the reference-facing call: pinned host tokens in (read in place by the
+        # mapping kernel), statistics and the trained input table out (as the reference's
+        # my_saveModel reads it), into pinned memory that the widening kernel writes in
+        # place.  Untimed calls first, as many as the headline's warm-up: the first GPU
+        # access to a pinned buffer sets up its host-page translations (about 0.2 s for
+        # 3.2 GB), and the first timed call after a single warm-up still paid about 90 ms.
         emb_host = torch.empty((wl["V"], TRAIN["size"]), dtype=torch.float32, pin_memory=True)
-        tr.train_corpus_ptr(corpus_host.data_ptr(), n_tok)
-        tr.embeddings_to(0, emb_host.data_ptr())
+        e2e_warm = max(1, args.warmup)
+        for _ in range(e2e_warm):
+            tr.train_corpus_ptr(corpus_host.data_ptr(), n_tok)
+            tr.embeddings_to(0, emb_host.data_ptr())
         e2e_t, e2e_pairs, e2e_kernel_ms = [], 0, []
         for it in range(max(1, args.steps)):
             torch.cuda.synchronize()
@@ -930,10 +934,10 @@ def main():
                        "d2h_bytes_per_step": 96 + 4 * wl["V"] * TRAIN["size"],
                        "read_back": "statistics and the trained Wih (fp32, V x d) through sgns_get_embeddings",
                        "outside_kernel_ms_per_step": 1e3 * float(np.mean(e2e_t)) - float(np.mean(e2e_kernel_ms))}
-        line["e2e"]["warmup"] = 1
-        # per e2e step: id->row mapping, longest-walk scan, training launch, the chunked
-        # bf16 -> fp32 widening of Wih (V*d / 8M elements per launch)
-        widen = -(-wl["V"] * TRAIN["size"] // (8 << 20))
+        line["e2e"]["warmup"] = e2e_warm
+        # per e2e step: id->row mapping, longest-walk scan, training launch, and the bf16 ->
+        # fp32 widening of Wih straight into the pinned buffer (one launch)
+        widen = 1
         line["gpu_launches"] = args.steps + (3 + widen) * max(1, args.steps)
         tr.close()
         del emb_host

@@ -1090,8 +1090,22 @@ sgns_status sgns_get_embeddings(sgns_handle* h, int32_t which, float* out) {
   const size_t n = (size_t)h->V * h->opt.size;
   const void* src = which ? h->woh : h->wih;
   if (h->opt.storage == SGNS_STORE_BF16_SR) {
-    // widened on the device in chunks through a small staging buffer, so the host receives
-    // fp32 rows directly (no host-side conversion of V*d elements)
+    // Pinned host memory mapped into this device's address space (16-byte aligned) is
+    // written in place by the widening kernel: the fp32 rows cross the host link once,
+    // with no staging buffer and no copy.
+    cudaPointerAttributes a{};
+    const bool mapped = cudaPointerGetAttributes(&a, out) == cudaSuccess && a.type == cudaMemoryTypeHost &&
+                        a.devicePointer != nullptr && a.device == h->opt.device &&
+                        (reinterpret_cast<uintptr_t>(a.devicePointer) & 15) == 0;
+    cudaGetLastError();  // a failed attribute query leaves no error behind
+    if (mapped) {
+      cudaError_t e = launch_widen_bf16(src, static_cast<float*>(a.devicePointer), (int64_t)n, h->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+      if (e != cudaSuccess) return fail(h, SGNS_ECUDA, "reading embeddings: %s", cudaGetErrorString(e));
+      return SGNS_OK;
+    }
+    // otherwise widened on the device in chunks through a small staging buffer, so the
+    // host receives fp32 rows directly (no host-side conversion of V*d elements)
     const size_t chunk = std::min<size_t>(n, (size_t)8 << 20);
     float* stage = nullptr;
     CU(h, cudaMalloc(&stage, chunk * 4));

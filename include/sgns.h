@@ -164,7 +164,9 @@ sgns_status sgns_get_stats(const sgns_handle* h, sgns_stats* out);
 int64_t sgns_vocab_size(const sgns_handle* h);
 /* Row -> vertex id of the frequency-sorted rows (v_vocab[r].id). */
 sgns_status sgns_get_order(const sgns_handle* h, uint32_t* order_out);
-/* which: 0 = Wih (the written embedding), 1 = Woh.  V*d floats in sorted-row order. */
+/* which: 0 = Wih (the written embedding), 1 = Woh.  V*d floats in sorted-row order.  BF16
+ * tables are widened on the device; when out is 16-byte aligned pinned host memory mapped
+ * for the handle's device, the widening kernel writes it in place (no staging copy). */
 sgns_status sgns_get_embeddings(sgns_handle* h, int32_t which, float* out);
 /* Overwrites Wih/Woh (sorted-row order, V*d floats; rounded to nearest for bf16). */
 sgns_status sgns_set_embeddings(sgns_handle* h, int32_t which, const float* in);

@@ -277,6 +277,29 @@ def test_pinned_host_corpus_is_read_in_place(sgns_lib):
         assert e.value.status == sgns.EINVAL
 
 
+def test_embeddings_into_pinned_host_memory(sgns_lib):
+    """BF16 tables read into pinned host memory (16-byte aligned: written in place by the
+    widening kernel; 4 bytes in: through the staging buffer) equal the read into pageable
+    memory, bit for bit."""
+    import torch
+
+    cfg, corpus, _ = case("cl_d128")
+    counts = np.bincount(corpus[corpus >= 0], minlength=cfg["V"]).astype(np.int32)
+    opt = sgns.default_options(size=cfg["d"], window=cfg["window"], negative=cfg["negative"], iter=1,
+                               sample=cfg["sample"], alpha=cfg["alpha"], engine="persistent", storage="bf16",
+                               table_size=1000000, debug=0)
+    with sgns.Trainer(opt) as t:
+        t.set_vocab(counts)
+        t.train_corpus(corpus)
+        for which in (0, 1):
+            want = t.embeddings(which)
+            pinned = torch.full((want.size + 4,), float("nan"), dtype=torch.float32, pin_memory=True)
+            for off in (0, 1):
+                t.embeddings_to(which, pinned.data_ptr() + 4 * off)
+                got = pinned[off:off + want.size].numpy().reshape(want.shape)
+                assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (which, off)
+
+
 @pytest.mark.parametrize("seed", [101, 303, 1002, 1003, 2054, 2192])
 @pytest.mark.parametrize("engine,storage", [("plain", "fp32"), ("persistent", "fp32"), ("persistent", "bf16")])
 def test_engines_match_oracle_on_random_configs(seed, engine, storage, sgns_lib, oracle_mod):
