@@ -320,7 +320,7 @@ def sbm_corpus_on_gpu(V, case, fx):
 
 def auc_suite(sizes=None, persistent_workers=0, plain_workers=0, plain_all_seeds=False):
     """Link-prediction AUC of every GPU engine on exactly the corpora of the committed CPU
-    fixture (tests/golden/auc_sbm.json: the survey's configuration 2 -- 4-block SBM, 10%
+    fixture (tests/golden/auc_sbm.json: configuration 2 -- 4-block SBM, 10%
     holdout, 10 information-oriented walks per vertex -- at 100k and 1.1M vertices, one
     graph/holdout/walk seed triple per case), against the CPU trainer's AUC recorded there.
     The plain fp32 engine (one launch per step, minutes per corpus) runs on the first seed of

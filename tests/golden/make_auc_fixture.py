@@ -1,7 +1,7 @@
 """Link-prediction AUC of the CPU trainer on fixed SBM corpora -- the fixture that the GPU
 engines' AUC is compared with (bench.py's auc_sbm leg, tests/test_gpu_auc.py).
 
-The survey's configuration 2: a 4-block stochastic block model (p_in / p_out = 20, about
+Configuration 2: a 4-block stochastic block model (p_in / p_out = 20, about
 2.73 undirected edges per vertex), 10% of the edges held out as in src/tools/gtrain.cpp
 :293-333, 10 information-oriented walks per vertex (the entropy/length stop rule of
 include/walk.hpp:260-387, 868-874, min length 20, capped at 80 vertices, R threshold 0.84

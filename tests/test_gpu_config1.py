@@ -1,4 +1,4 @@
-"""Configuration 1 as the survey states it: a seeded Chung-Lu graph of 10,000 vertices and
+"""Configuration 1 at its stated size: a seeded Chung-Lu graph of 10,000 vertices and
 about 100,000 edges (exponent 2.1), 10 uniform random walks of length 80 per vertex
 (8 million tokens), d = 128, window 10, 5 negatives, batch 21, sample 1e-3, alpha 0.01
 with linear decay, one pass, a 1e7-entry unigram table.  Replay-exact mode (one worker,

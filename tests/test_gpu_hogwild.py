@@ -8,7 +8,7 @@ with no negatives (-negative 0: the outputs are the two walks' targets) and fewe
 10,000 tokens per worker (no learning-rate update, which sums all workers' progress,
 dsgl.hpp:886-897).  Every row is then written by one worker only, so the GPU engines, with
 all workers in flight at once, must give the oracle's rows at the same worker count: the
-survey's per-row tolerance under Hogwild ordering is 1e-5 relative, and here the order of
+per-row tolerance under Hogwild ordering is 1e-5 relative, and here the order of
 each row's updates is fixed, so the rows are required bit for bit."""
 import numpy as np
 import pytest
