@@ -1,5 +1,5 @@
 """Link-prediction AUC of the CPU trainer on fixed SBM corpora -- the fixture that the GPU
-engines' AUC is compared with (bench.py's auc_sbm leg, tests/test_gpu_auc.py).
+engines' AUC is compared with (bench.py's auc_sbm leg).
 
 Configuration 2: a 4-block stochastic block model (p_in / p_out = 20, about
 2.73 undirected edges per vertex), 10% of the edges held out as in src/tools/gtrain.cpp
